@@ -1,0 +1,402 @@
+"""Benchmark of the GB300 hex8 linear-elastic solve path.
+
+Workload (one "step" = one full solve from the assembled, eliminated K, RHS
+and boundary conditions resident in HBM to x at the tolerance):
+  lognormal100 -- Cube3D 100^3 hex8 (1,030,301 nodes, 3,090,903 DOF), per-element
+  E = exp(N(ln 1e4, 0.5^2)) (numpy default_rng seed 20261203), nu = 0.3,
+  z = 0 fixed, traction -1 z on top as consistent nodal loads; CG with 3x3
+  block-Jacobi, FP32 inner iterations + FP64 residual replacement, stopped on
+  the FP64 relative residual |b - Kx|/|b| <= 1e-10.
+
+Reported next to it (same JSON line): the plain FP64 GPU solve, the FP64 and
+FP32 block SpMV bandwidth, the end-to-end solve through the C ABI's
+LinearSolver plug-in with host CRS arrays, and the CPU oracle port of the
+reference's bicgstab_CRS_2 timed on the host cores.
+
+``--impl reference`` times the reference algorithm itself on the host CPU
+(the oracle's restatement of bicgstab_CRS_2 with the per-nonzero OpenMP
+atomic SpMV; the reference's Fortran cannot be compiled on these machines).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 100
+TOL = 1e-10
+# Iterations the reference algorithm (unpreconditioned bicgstab_CRS_2, FP64,
+# reference stop rule sqrt(rr/rr_1) < 1e-10) needs on lognormal100, measured
+# with this library's FP64 BiCGSTAB on a GB300 (same algorithm and stop rule).
+# The CPU arm times a bounded sample of iterations and scales by this count.
+REF_ITERS_LOGNORMAL100 = None
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------- our arm
+def run_ours(args, ws, rank, local):
+    import torch
+    import plantfem_gb300 as P
+    from plantfem_gb300 import FEMSolver, _native, linear_solver_crs, problems
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n
+    t0 = time.perf_counter()
+    p = problems.lognormal(n)
+    dom = p["domain"]
+    s = FEMSolver()
+    s.setDomain(dom)
+    s.setCRS(3)
+    torch.cuda.synchronize()
+    t_pat = time.perf_counter()
+    s.assembleStiffness(p["E"], p["nu"])
+    t_asm = time.perf_counter()
+    s.setRHS(p["rhs"])
+    s.fix(1, p["fix_ids"], FixValue=0.0)
+    s.relative_er = TOL
+    # first solve applies the Dirichlet elimination (FEMSolver_%solve semantics)
+    x64_host = s.solve(algorithm="CG", preconditioning="BlockJacobi", precision="fp64", stop_rule="true_relative")
+    info64_first = dict(s.last_info)
+    ndof = x64_host.shape[0]
+    b = torch.tensor(s.CRS_RHS, dtype=torch.float64, device=dev)
+    x = torch.zeros(ndof, dtype=torch.float64, device=dev)
+    x_ref = torch.tensor(x64_host, dtype=torch.float64, device=dev)
+    setup_s = time.perf_counter() - t0
+
+    def solve_once(precision, algorithm="CG", pc="BlockJacobi"):
+        x.zero_()
+        return s.solve_device(b, x, algorithm=algorithm, preconditioning=pc, precision=precision,
+                              stop_rule="true_relative")
+
+    for _ in range(args.warmup):
+        solve_once("mixed")
+    torch.cuda.synchronize()
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    infos = []
+    torch.cuda.synchronize()
+    ev0.record()
+    for _ in range(args.steps):
+        infos.append(solve_once("mixed"))
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_total = ev0.elapsed_time(ev1)
+    clk = clocks.stop()
+    barrier(ws)
+    ms_total = max_over_ranks(ms_total, ws)
+    ms_step = ms_total / args.steps
+    value = ws * args.steps / (ms_total / 1e3)
+    err_mixed = float(torch.linalg.norm(x - x_ref) / torch.linalg.norm(x_ref))
+    mixed_info = infos[-1]
+
+    # plain FP64 GPU path (same algorithm, preconditioner and stop rule)
+    f64_steps = max(1, min(args.steps, 3))
+    solve_once("fp64")
+    ev0.record()
+    f64_infos = [solve_once("fp64") for _ in range(f64_steps)]
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_f64 = ev0.elapsed_time(ev1) / f64_steps
+
+    out_extra = {}
+    # reference algorithm on the GPU: unpreconditioned BiCGSTAB, reference stop rule
+    if not args.skip_bicgstab:
+        x.zero_()
+        ib = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64",
+                            stop_rule="reference")
+        out_extra["bicgstab_fp64_reference_rule"] = {"iterations": ib["iterations"], "ms": ib["solve_ms"],
+                                                     "rel_residual": ib["rel_residual"], "status": ib["status"]}
+        x.zero_()
+        im = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="mixed",
+                            stop_rule="true_relative")
+        x.zero_()
+        i64 = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64",
+                             stop_rule="true_relative")
+        out_extra["bicgstab_true_rel_1e-10"] = {
+            "mixed": {"ms": im["solve_ms"], "iterations": im["iterations"], "status": im["status"]},
+            "fp64": {"ms": i64["solve_ms"], "iterations": i64["iterations"], "status": i64["status"]},
+            "speedup_mixed_vs_fp64": i64["solve_ms"] / im["solve_ms"] if im["solve_ms"] > 0 else None}
+
+    # kernel roofline: the dominant kernel of the mixed solve is the FP32 block
+    # SpMV with the fused direction update (k_cg_spmv<3,float>)
+    prof = {}
+    for kid, name in ((0, "spmv_fp64"), (1, "spmv_fp32"), (2, "cg_spmv_fp32_fused")):
+        import ctypes as C
+        ms, by = C.c_double(), C.c_double()
+        _native.check(_native.load().pfg_profile_kernel(s.handle, kid, 20, C.byref(ms), C.byref(by)))
+        prof[name] = {"ms": ms.value, "bytes": by.value, "GBs": by.value / (ms.value * 1e-3) / 1e9}
+    pk = peaks()
+    peak = pk["hbm_gbs"] if pk else 6800.0
+    dom_k = prof["cg_spmv_fp32_fused"]
+    roofline = {"kernel": "k_cg_spmv<3,float> (FP32 3x3-block SpMV + fused p update + p.q)", "bound": "hbm",
+                "achieved": round(dom_k["GBs"], 1), "peak": peak, "unit": "GB/s",
+                "frac": round(dom_k["GBs"] / peak, 4), "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk else "fallback 6800 GB/s"}
+
+    # end to end through the C ABI plug-in with host (pinned) CRS arrays
+    e2e = None
+    if not args.skip_e2e:
+        rp, ci, val = s.getCRS()
+        rp_p = torch.from_numpy(rp).pin_memory()
+        ci_p = torch.from_numpy(ci).pin_memory()
+        val_p = torch.from_numpy(val).pin_memory()
+        rhs_p = torch.from_numpy(s.CRS_RHS).pin_memory()
+        xh = torch.zeros(ndof, dtype=torch.float64).pin_memory()
+        rpn, cin, valn, rhsn, xn = rp_p.numpy(), ci_p.numpy(), val_p.numpy(), rhs_p.numpy(), xh.numpy()
+        xn[:] = 0
+        linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL)  # warm-up: allocations, graphs
+        e2e_steps = max(1, min(args.steps, 3))
+        t_a = time.perf_counter()
+        e2e_infos = []
+        for _ in range(e2e_steps):
+            xn[:] = 0
+            e2e_infos.append(linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL))
+        t_e2e = (time.perf_counter() - t_a) / e2e_steps
+        h2d = rpn.nbytes + cin.nbytes + valn.nbytes + rhsn.nbytes + xn.nbytes
+        e2e = {"value": round(ws / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(xn.nbytes), "ms_per_step": round(t_e2e * 1e3, 2),
+               "path": "pfg_linear_solver_crs (FEMSolver_%solve LinearSolver hook) with pinned host CRS",
+               "rel_err_vs_fp64": float(np.linalg.norm(xn - x64_host) / np.linalg.norm(x64_host))}
+        del rp_p, ci_p, val_p
+
+    # CPU baseline: the oracle's bicgstab_CRS_2 restatement on the host cores
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        cpu = cpu_baseline_sample(s, out_extra.get("bicgstab_fp64_reference_rule", {}).get("iterations"))
+
+    launches = int(sum(i["kernel_launches"] for i in infos))
+    line = {
+        "metric": "solves/s of the 3,090,903-DOF hex8 elasticity solve at 1e-10 relative residual "
+                  "(mixed FP32/FP64 CG vs FP64), plus block-SpMV HBM GB/s",
+        "value": round(value, 4), "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 inner / f64 residual", "data": "synthetic (seeded lognormal E, numpy seed 20261203)",
+        "config": {"workload": f"lognormal{n}: Cube3D {n}^3 hex8, {ndof} DOF, E~lognormal(ln1e4, 0.5), nu 0.3, "
+                               "z=0 fixed, top traction -1; CG + 3x3 block Jacobi; rel. residual 1e-10",
+                   "l2": "inputs larger than L2 (FP32 matrix 1.1 GB read per SpMV)",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "mixed": {"iterations": mixed_info["iterations"], "replacements": mixed_info["replacements"],
+                  "rel_residual": mixed_info["rel_residual"], "rel_err_vs_fp64": err_mixed,
+                  "ms": round(ms_step, 3)},
+        "fp64": {"solves_per_s": round(1e3 / ms_f64, 4), "ms": round(ms_f64, 3),
+                 "iterations": f64_infos[-1]["iterations"], "rel_residual": f64_infos[-1]["rel_residual"]},
+        "speedup_mixed_vs_fp64": round(ms_f64 / ms_step, 3),
+        "spmv": {k: {"GBs": round(v["GBs"], 1), "ms": round(v["ms"], 4), "bytes": v["bytes"]} for k, v in prof.items()},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "setup": {"total_s": round(setup_s, 2), "pattern_and_mesh_s": round(t_pat - t0, 2),
+                  "assembly_s": round(t_asm - t_pat, 3)},
+        **out_extra,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(s, ref_iters):
+    """Oracle port of bicgstab_CRS_2 (OpenMP, atomic SpMV) on the host cores:
+    a bounded sample of iterations, scaled to the iteration count the
+    reference algorithm needs on this system."""
+    import oracle as O
+    rp, ci, val = s.getCRS()
+    b = s.CRS_RHS
+    k = 4
+    t = time.perf_counter()
+    O.bicgstab_crs2(rp, ci, val, b, itrmax=k, relative_er=1e-300, er0=1e-300, atomic=True)
+    t_it = (time.perf_counter() - t) / k
+    iters = ref_iters or REF_ITERS_LOGNORMAL100
+    return {"value": round(1.0 / (t_it * iters), 8) if iters else None, "unit": "solves/s",
+            "cores": O.num_threads(), "kind": "port",
+            "sample": f"{k} iterations of bicgstab_CRS_2 (oracle C/OpenMP restatement, per-nonzero atomic SpMV) "
+                      f"on the eliminated scalar CRS: {t_it * 1e3:.1f} ms/iteration, scaled to "
+                      f"{iters} iterations (the count the same algorithm and stop rule take on the GPU)",
+            "ms_per_iteration": round(t_it * 1e3, 2)}
+
+
+# ------------------------------------------------------------ reference arm
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import oracle as O
+    from plantfem_gb300 import problems
+
+    n = args.n
+    xyz, en = O.cube3d(n, n, n)
+    nn = xyz.shape[0]
+    E = problems.lognormal_E(en.shape[0])
+    rp, ci = O.zero_matrix(nn, en, 3)
+    val = O.assemble(xyz, en, rp, ci, "stiffness", E=E, nu=0.3)
+    dom_rhs = _traction_rhs(xyz, en, n)
+    fixed = np.zeros(3 * nn, np.uint8)
+    bot = np.nonzero(xyz[:, 2] <= 0.0)[0]
+    for d in range(3):
+        fixed[3 * bot + d] = 1
+    b = dom_rhs.copy()
+    O.apply_fix(rp, ci, val, b, fixed, np.zeros(3 * nn))
+    k = 2
+    for _ in range(args.warmup):
+        O.bicgstab_crs2(rp, ci, val, b, itrmax=1, relative_er=1e-300, er0=1e-300, atomic=True)
+    times = []
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        O.bicgstab_crs2(rp, ci, val, b, itrmax=k, relative_er=1e-300, er0=1e-300, atomic=True)
+        times.append((time.perf_counter() - t) / k)
+    t_it = statistics.median(times)
+    iters = REF_ITERS_LOGNORMAL100
+    value = 1.0 / (t_it * iters) if iters else None
+    sample = (f"each step: {k} iterations of bicgstab_CRS_2 (oracle C/OpenMP restatement with the per-nonzero "
+              f"atomic SpMV of LinearSolverClass.f90:3766-3774) on lognormal{n}; {t_it * 1e3:.1f} ms/iteration "
+              f"scaled to {iters} iterations")
+    line = {"impl": "reference", "metric": "solves/s of the 3,090,903-DOF hex8 elasticity solve at 1e-10 relative "
+                                           "residual (mixed FP32/FP64 CG vs FP64), plus block-SpMV HBM GB/s",
+            "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t_it * 1e3 * k, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded lognormal E, numpy seed 20261203)",
+            "config": {"workload": f"lognormal{n}: Cube3D {n}^3 hex8, {3 * nn} DOF; reference bicgstab_CRS_2, FP64"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": O.num_threads(), "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _traction_rhs(xyz, en, n, t=-1.0):
+    rhs = np.zeros(xyz.shape[0] * 3)
+    top = en[:, 4:8] - 1
+    on = np.all(xyz[top, 2] >= xyz[:, 2].max(), axis=1)
+    f = top[on]
+    a = (1.0 / n) ** 2
+    np.add.at(rhs, 3 * f.ravel() + 2, t * a / 4.0)
+    return rhs
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT, help="elements per cube edge (100 = the benchmark)")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-bicgstab", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_setup()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * pfg.h -- C ABI of plantfem_gb300, the GB300-native (sm_103a) linear-elastic
+ * hex8 solve path of plantFEM.
+ *
+ * Every entry point is a plain C function over plain pointers and sizes; no
+ * C++ or torch types cross this boundary.  Functions return 0 (PFG_OK) on
+ * success, a positive PFG_W_* warning, or a negative PFG_E_* error code; the
+ * text of the last error on the calling thread is pfg_last_error().  Nothing
+ * here exits the process (the reference prints and `stop`s instead).
+ *
+ * Numbering follows the reference: node, element and DOF ids passed in are
+ * 1-based; CRS arrays are 1-based int64 row pointers and int32 column indices
+ * in first-appearance column order, exactly as FEMSolver_%CRS_Index_Row /
+ * CRS_Index_Col (FEMSolverClass.f90:25-27).  Mesh arrays are Fortran
+ * column-major: NodCoord(nn,3) and ElemNod(ne,8).
+ *
+ * Each declaration names the reference routine it replaces (file:line inside
+ * the plantFEM tree).
+ */
+#ifndef PFG_H
+#define PFG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------- status codes */
+#define PFG_OK 0
+#define PFG_W_NOT_CONVERGED 1   /* itrmax reached ("[ERROR] LOBPCG NOT CONVERGED", SparseClass.f90:2237) */
+#define PFG_E_ARG (-1)          /* bad argument (size, NULL, out of range) */
+#define PFG_E_STATE (-2)        /* call order (e.g. solve before setCRS) */
+#define PFG_E_MISSING_SLOT (-3) /* fill-in request, FEMSolverClass.f90:1040-1047 */
+#define PFG_E_BREAKDOWN (-4)    /* "Bicgstab devide by zero", FEMSolverClass.f90:2266,2295 */
+#define PFG_E_NOMEM (-5)        /* device or host allocation failed */
+#define PFG_E_CUDA (-6)         /* CUDA runtime error */
+#define PFG_E_DETJ (-7)         /* zero-volume element, "Bmat,detJ=0" FEMDomainClass.f90:12285 */
+#define PFG_E_INTERNAL (-8)
+#define PFG_E_UNSUPPORTED (-9)
+#define PFG_E_NONFINITE (-10)   /* NaN/Inf in the input or in a Krylov scalar */
+
+/* ----------------------------------------------------------- solve options */
+#define PFG_ALG_BICGSTAB 0      /* bicgstab_CRS_2, FEMSolverClass.f90:2199-2298 (reference default) */
+#define PFG_ALG_CG 1            /* conjugate gradients (K is symmetric after elimination) */
+
+#define PFG_PREC_FP64 0         /* every operation in FP64 (the plain drop-in) */
+#define PFG_PREC_MIXED 1        /* FP32 inner iterations, FP64 residual replacement */
+
+#define PFG_PC_NONE 0           /* unpreconditioned, as the reference */
+#define PFG_PC_JACOBI 1         /* point Jacobi (JacobiPreconditionerCRS, FEMSolverClass.f90:2508-2529) */
+#define PFG_PC_BLOCK_JACOBI 2   /* inverse of each 3x3 diagonal node block */
+
+#define PFG_STOP_REFERENCE 0    /* sqrt(rr/rr_1) < relative_er or sqrt(rr) < er0, FEMSolverClass.f90:2275-2289 */
+#define PFG_STOP_TRUE_RELATIVE 1 /* |b - A x| / |b| <= relative_er, with |b - A x| recomputed in FP64 */
+
+typedef struct pfg_solve_opts {
+    int32_t algorithm;       /* PFG_ALG_* */
+    int32_t precision;       /* PFG_PREC_* */
+    int32_t precond;         /* PFG_PC_* */
+    int32_t stop_rule;       /* PFG_STOP_* (mixed precision always uses TRUE_RELATIVE) */
+    int32_t itrmax;          /* FEMSolver_%itrmax, default 100000 (FEMSolverClass.f90:69) */
+    int32_t graph_chunk;     /* iterations per captured CUDA graph launch, default 32 */
+    double er0;              /* FEMSolver_%er0, default 1e-10 (FEMSolverClass.f90:70) */
+    double relative_er;      /* FEMSolver_%relative_er, default 1e-10 (FEMSolverClass.f90:71) */
+    double reliable_delta;   /* mixed: replace the FP32 residual by the FP64 one whenever it fell
+                                by this factor since the last replacement; default 0.1 */
+    int32_t debug;           /* FEMSolver_%debug: print the residual per graph chunk */
+    int32_t reserved;
+} pfg_solve_opts;
+
+typedef struct pfg_info {
+    int32_t status;          /* PFG_OK, PFG_W_NOT_CONVERGED or PFG_E_BREAKDOWN */
+    int32_t iterations;      /* Krylov iterations */
+    int32_t replacements;    /* mixed: FP64 residual replacements */
+    int32_t kernel_launches; /* kernels this call launched (directly or inside CUDA graphs) */
+    double rel_residual;     /* |b - A x| / |b| recomputed in FP64 at exit */
+    double iter_residual;    /* recursive residual the stop rule saw */
+    double solve_ms;         /* device time of the solve */
+} pfg_info;
+
+/* Fill opts with the reference's defaults (BiCGSTAB, FP64, no preconditioner,
+ * reference stop rule, itrmax 100000, er0 = relative_er = 1e-10). */
+void pfg_solve_opts_default(pfg_solve_opts *opts);
+
+const char *pfg_last_error(void);
+const char *pfg_version(void);
+
+/* --------------------------------------------------------------- handle */
+typedef struct pfg_solver pfg_solver;
+
+/* FEMSolver_%init(NumDomain=1) (FEMSolverClass.f90:174-327) on the current
+ * CUDA device.  One handle = one stream; calls on a handle are serialised. */
+int pfg_create(pfg_solver **h);
+/* FEMSolver_%remove() (FEMSolverClass.f90:1827-1889): frees everything. */
+int pfg_destroy(pfg_solver *h);
+
+/* FEMSolver_%setDomain(FEMDomain, DomainID=1) (FEMSolverClass.f90:329-419):
+ * copies the hex8 mesh to the device.  nodcoord: NodCoord(nn,3) column-major;
+ * elemnod: ElemNod(ne,nne) column-major, 1-based, nne must be 8. */
+int pfg_set_mesh(pfg_solver *h, int64_t nn, const double *nodcoord, int64_t ne, int32_t nne,
+                 const int32_t *elemnod);
+
+/* FEMSolver_%setCRS(DOF) (FEMSolverClass.f90:439-898, single-domain branch
+ * :677-694 -> ZeroMatrix_as_CRS FEMDomainClass.f90:10581-10840): builds the
+ * sparsity pattern on the device; values and RHS start at zero.  dof must be 3. */
+int pfg_set_crs(pfg_solver *h, int32_t dof);
+
+/* FEMSolver_%setCRS(CRS_) (FEMSolverClass.f90:421-429): adopt a caller CRS
+ * (1-based).  Matrices with the 3x3 node-block structure of ZeroMatrix are
+ * stored as 3x3 blocks, any other matrix as 1x1 blocks. */
+int pfg_set_crs_arrays(pfg_solver *h, int64_t n, const int64_t *row_ptr, const int32_t *col_idx,
+                       const double *val);
+
+/* Size of the scalar CRS of the working matrix (n rows, nnz entries). */
+int pfg_get_crs_size(pfg_solver *h, int64_t *n, int64_t *nnz);
+/* FEMSolver_%getCRS() (FEMSolverClass.f90:2690-2727) / the public CRS_Index_Row,
+ * CRS_Index_Col, CRS_val fields: copy the working matrix out as 1-based scalar
+ * CRS in the reference's column order.  Any pointer may be NULL. */
+int pfg_get_crs(pfg_solver *h, int64_t *row_ptr, int32_t *col_idx, double *val);
+
+/* FEMSolver_%setRHS(RHS) (FEMSolverClass.f90:431-437). */
+int pfg_set_rhs(pfg_solver *h, int64_t n, const double *rhs);
+/* Copy the current RHS (after elimination, if a solve ran) out. */
+int pfg_get_rhs(pfg_solver *h, int64_t n, double *rhs);
+
+/* FEMSolver_%setMatrix(DomainID, ElementID, DOF, Matrix) (FEMSolverClass.f90:901-911
+ * -> setValue :1020-1057): add a 24x24 column-major element matrix.  Additions are
+ * buffered on the host and scattered on the device at the next call that reads
+ * the matrix. */
+int pfg_set_matrix(pfg_solver *h, int32_t domain_id, int32_t element_id, int32_t dof, const double *matrix);
+/* Batched form: count element matrices, element_ids 1-based, matrices count*576. */
+int pfg_set_matrices(pfg_solver *h, int64_t count, const int32_t *element_ids, const double *matrices);
+/* FEMSolver_%setVector(DomainID, ElementID, DOF, Vector) (FEMSolverClass.f90:913-920,
+ * setValue :1059-1069): add a 24-entry element vector to the RHS. */
+int pfg_set_vector(pfg_solver *h, int32_t domain_id, int32_t element_id, int32_t dof, const double *vector);
+
+/* Element loop + scatter of StiffnessMatrixFEMDomain(ElementID, E, v)
+ * (FEMDomainClass.f90:11457-11515) over all elements, on the device, with
+ * graph-coloured atomic-free scatter; the whole-matrix form of
+ * StiffnessMatrix_as_CRS (FEMDomainClass.f90:11123-11232).  E, nu: ne values
+ * (or 1 value broadcast when n_prop == 1).  Adds into the working matrix. */
+int pfg_assemble_stiffness(pfg_solver *h, int64_t n_prop, const double *E, const double *nu);
+/* Same for MassMatrixFEMDomain(ElementID, Density, DOF=3) (FEMDomainClass.f90:10874-10952);
+ * lumped != 0 applies the row lumping of :10940-10948. */
+int pfg_assemble_mass(pfg_solver *h, int64_t n_prop, const double *rho, int32_t lumped);
+/* Same for MassVectorFEMDomain(ElementID, Density, DOF=3, Accel) (FEMDomainClass.f90:10993-11073)
+ * summed into the RHS, as the tutorials' setVector loop does. */
+int pfg_assemble_body_force(pfg_solver *h, int64_t n_prop, const double *rho, const double accel[3]);
+
+/* FEMSolver_%zeros() (FEMSolverClass.f90:1310-1322): zero values and RHS. */
+int pfg_zeros(pfg_solver *h);
+
+/* FEMSolver_%fix(DomainID, IDs, FixValue | FixValues) (FEMSolverClass.f90:1073-1136):
+ * mark 1-based DOF ids fixed; values NULL -> every id gets `value`.  Ids < 1 or
+ * beyond the system size are skipped, as the reference's first call does. */
+int pfg_fix(pfg_solver *h, int64_t n, const int32_t *ids, const double *values, double value);
+
+/* x = FEMSolver_%solve() (FEMSolverClass.f90:1697-1825): Dirichlet elimination
+ * (mutates the stored matrix and RHS in place, as the reference), Krylov solve,
+ * x(fixed) = value.  opts NULL -> pfg_solve_opts_default.  x0 may be NULL.
+ * x_out receives n values; info may be NULL. */
+int pfg_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *x0, double *x_out, pfg_info *info);
+
+/* ------------------------------------------------ reference-signature plug-ins */
+/* crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector, n, col_size)
+ * (SparseClass-c.c:131-143, bound at SparseClass.f90:38-51): new_vector += A *
+ * old_vector on the GPU; host arrays, 1-based row_ptr/col_idx. */
+int pfg_crs_spmv_real64(const double *val, const int64_t *row_ptr, const int32_t *col_idx,
+                        const double *old_vector, double *new_vector, size_t n, size_t col_size);
+/* crs_spmv_real32 (SparseClass-c.c:116-128, bound at SparseClass.f90:25-36). */
+int pfg_crs_spmv_real32(const float *val, const int64_t *row_ptr, const int32_t *col_idx,
+                        const float *old_vector, float *new_vector, size_t n, size_t col_size);
+
+/* The user-solver hook of FEMSolver_%solve(LinearSolver=..., x0) (FEMSolverClass.f90:1632-1662):
+ * subroutine LinearSolver(row_ptr, col_idx, val, rhs, x) over host CRS arrays
+ * (1-based), x in/out (x0 on entry).  n = size(rhs), nnz = size(val). */
+int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const double *val, const double *rhs,
+                          double *x, int64_t n, int64_t nnz, const pfg_solve_opts *opts, pfg_info *info);
+
+/* ------------------------------------------------ device-pointer entry points */
+/* For callers that already hold device memory (the PyTorch binding): the same
+ * operations over device pointers on a caller stream (cudaStream_t as void*). */
+/* y = K x (FP64) with the handle's working matrix. */
+int pfg_dev_spmv(pfg_solver *h, const double *d_x, double *d_y, void *stream);
+/* Solve with the handle's (already eliminated) matrix: d_b -> d_x (x0 on entry). */
+int pfg_dev_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *d_b, double *d_x, pfg_info *info,
+                  void *stream);
+
+/* ------------------------------------------------------------ instrumentation */
+/* No counterpart in the reference (it has only wall-clock timers, TimeClass.f90).
+ * Times `reps` back-to-back launches of one kernel on the handle's matrix with
+ * CUDA events on the handle's stream and returns the mean milliseconds per
+ * launch and the algorithmic bytes one launch moves.  kernel: 0 = FP64 block
+ * SpMV, 1 = FP32 block SpMV, 2 = the FP32 CG SpMV with the fused direction
+ * update (the dominant kernel of the mixed-precision solve). */
+int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, double *ms_per_launch, double *bytes_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFG_H */

@@ -1,0 +1,103 @@
+"""numpy restatement of plantFEM's LOBPCG_CRS (TEST INFRASTRUCTURE ONLY).
+
+Follows ``src/SparseClass/SparseClass.f90:2008-2239`` step by step, with
+``GramSchmidt`` (``:2243-2275``) restated literally and LAPACK ``DSPGVD``
+(ITYPE=1, JOBZ='V', UPLO='U'; ``:2279-2351``) replaced by
+``scipy.linalg.eigh(a, b, type=1)``, which solves the same generalized
+symmetric-definite problem (ascending eigenvalues, B-normalised vectors).
+DSPGVD is an un-vendored LAPACK dependency (linked as ``-llapack`` in the
+reference's Makefile:8, no pinned version); scipy's bundled LAPACK stands in.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+
+
+def gram_schmidt(V: np.ndarray) -> np.ndarray:
+    """GramSchmidt (SparseClass.f90:2243-2275): column-sequential modified GS,
+    zero columns skipped, each column normalised after projection."""
+    out = V.copy()
+    m = out.shape[1]
+    for i in range(m):
+        viold = out[:, i].copy()
+        if np.dot(viold, viold) == 0.0:
+            continue
+        for j in range(i):
+            nai = np.dot(out[:, j], viold)
+            viold = viold - nai * out[:, j]
+        out[:, i] = viold / np.sqrt(np.dot(viold, viold))
+    return out
+
+
+def lapack_eig(A, B):
+    """LAPACK_EIG_DENSE via DSPGVD (ascending eigenvalues, B-orthonormal vectors)."""
+    w, Z = sla.eigh(0.5 * (A + A.T), 0.5 * (B + B.T), type=1)
+    return Z, w
+
+
+def lobpcg_crs(A, B, m: int, max_itr: int = 100000, tol: float = 1e-6, X_init=None, seed: int = 0,
+               return_iters: bool = False):
+    """LOBPCG_CRS(A, B, lambda, X, m, MAX_ITR, TOL, X_init) with A, B scipy sparse.
+
+    Convergence test as the reference: max|R| / max|R at iteration 1| < TOL
+    (SparseClass.f90:2218-2234).  The random start (``random%randn`` is
+    uniform, RandomClass.f90:265-283) uses a seeded numpy generator here.
+    """
+    n = A.shape[0]
+    rng = np.random.default_rng(seed)
+    X = rng.random((n, m)) if X_init is None else np.array(X_init, dtype=np.float64)
+    X = X / np.linalg.norm(X, axis=0)
+    X = gram_schmidt(X)
+    AX = A @ X
+    BX = B @ X
+    b_small, lam = lapack_eig(X.T @ AX, X.T @ BX)
+    X = X @ b_small
+    AX = A @ X
+    BX = B @ X
+    R = AX - BX * lam[None, :m]
+    V = gram_schmidt(np.hstack([X, R]))
+    V[:, :m] = V[:, :m] / np.linalg.norm(V[:, :m], axis=0)
+    X = V[:, :m].copy()
+    R = V[:, m:2 * m].copy()
+    AV = A @ V
+    BV = B @ V
+    b_small, lam = lapack_eig(V.T @ AV, V.T @ BV)
+    X = V @ b_small[:, :m]
+    AX = A @ X
+    BX = B @ X
+    R = AX - BX * lam[None, :m]
+    OR = np.hstack([np.zeros((n, m)), R])
+    P = OR @ b_small[:, :m]
+    initial_R = None
+    it = 0
+    for it in range(1, max_itr + 1):
+        V = gram_schmidt(np.hstack([X, R, P]))
+        V[:, :m] = V[:, :m] / np.linalg.norm(V[:, :m], axis=0)
+        V[:, 2 * m:] = V[:, 2 * m:] / np.linalg.norm(V[:, 2 * m:], axis=0)
+        AV = A @ V
+        BV = B @ V
+        b_small, lam = lapack_eig(V.T @ AV, V.T @ BV)
+        X = V @ b_small[:, :m]
+        AX = A @ X
+        BX = B @ X
+        R = AX - BX * lam[None, :m]
+        V[:, :m] = 0.0
+        P = V @ b_small[:, :m]
+        rmax = np.abs(R).max()
+        if it == 1:
+            initial_R = rmax
+        if rmax / initial_R < tol:
+            break
+    lam = lam[:m].copy()
+    if return_iters:
+        return lam, X, it
+    return lam, X
+
+
+def dense_generalized_eig(A, B, k: int):
+    """Lowest k eigenpairs of the dense pencil (DSPGVD stand-in) for small n."""
+    Ad = A.toarray() if hasattr(A, "toarray") else np.asarray(A)
+    Bd = B.toarray() if hasattr(B, "toarray") else np.asarray(B)
+    w, Z = sla.eigh(Ad, Bd, type=1, subset_by_index=(0, k - 1))
+    return w, Z

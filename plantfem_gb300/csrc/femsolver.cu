@@ -1,0 +1,653 @@
+// femsolver.cu -- the FEMSolver_ handle behind the C ABI (include/pfg.h).
+//
+// Mirrors the state of plantFEM's FEMSolver_ (FEMSolverClass.f90:13-164):
+// one domain (mesh), the working CRS matrix (CRS_val / CRS_Index_*), CRS_RHS,
+// the fix list (fix_lin_exists / fix_lin_exists_values), and the named matrix
+// stack of keepThisMatrixAs.  All of it lives on the device; host arrays are
+// copied in at set*/fix and out at solve/eig/getCRS, like the reference's
+// value-semantics setters.
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "assembly.cuh"
+
+namespace pfg {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+}  // namespace pfg
+
+using namespace pfg;
+
+struct pfg_solver {
+    std::mutex mu;
+    cudaStream_t st = nullptr;
+    int device = 0;
+    DevMesh mesh;
+    bool have_mesh = false;
+    DevMatrix K;
+    bool have_crs = false;
+    DevBuf<double> rhs;
+    std::vector<uint8_t> fixed_h;
+    std::vector<double> fixval_h;
+    bool have_fix = false;
+    DevBuf<uint8_t> fixed_d;
+    DevBuf<double> fixval_d;
+    // buffered setMatrix / setVector calls (0-based element ids)
+    std::vector<int> pend_mat_ids;
+    std::vector<double> pend_mats;
+    std::vector<int> pend_vec_ids;
+    std::vector<double> pend_vecs;
+    Krylov kry;
+    DevBuf<double> x;
+    // keepThisMatrixAs stack (FEMSolverClass.f90:1544-1604), at most 10 names
+    std::vector<std::pair<std::string, DevMatrix>> stack;
+    std::vector<int> fix_eig_ids;  // 1-based, unique, sorted (fix_eig, :1607-1628)
+
+    int64_t ndof() const { return K.ndof(); }
+};
+
+namespace {
+
+void need(bool c, int code, const char *msg)
+{
+    if (!c) throw Error(code, msg);
+}
+
+void flush_pending(pfg_solver *h)
+{
+    if (!h->pend_mat_ids.empty()) {
+        const int64_t cnt = (int64_t)h->pend_mat_ids.size();
+        DevBuf<int> ids((size_t)cnt);
+        DevBuf<double> mats((size_t)cnt * 576);
+        PFG_CUDA(cudaMemcpyAsync(ids.p, h->pend_mat_ids.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(mats.p, h->pend_mats.data(), cnt * 576 * sizeof(double), cudaMemcpyHostToDevice,
+                                 h->st));
+        scatter_element_matrices(h->mesh, h->K, cnt, ids.p, mats.p, h->st);
+        h->pend_mat_ids.clear();
+        h->pend_mats.clear();
+    }
+    if (!h->pend_vec_ids.empty()) {
+        const int64_t cnt = (int64_t)h->pend_vec_ids.size();
+        DevBuf<int> ids((size_t)cnt);
+        DevBuf<double> vecs((size_t)cnt * 24);
+        PFG_CUDA(cudaMemcpyAsync(ids.p, h->pend_vec_ids.data(), cnt * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(vecs.p, h->pend_vecs.data(), cnt * 24 * sizeof(double), cudaMemcpyHostToDevice,
+                                 h->st));
+        scatter_element_vectors(h->mesh, h->rhs.p, cnt, ids.p, vecs.p, h->st);
+        h->pend_vec_ids.clear();
+        h->pend_vecs.clear();
+    }
+}
+
+void reset_system(pfg_solver *h)
+{
+    const int64_t n = h->ndof();
+    h->rhs.alloc((size_t)std::max<int64_t>(n, 1));
+    PFG_CUDA(cudaMemsetAsync(h->rhs.p, 0, n * sizeof(double), h->st));
+    h->fixed_h.assign((size_t)n, 0);
+    h->fixval_h.assign((size_t)n, 0.0);
+    h->have_fix = false;
+    h->have_crs = true;
+}
+
+// setCRS(DOF): pattern from the mesh
+void set_crs_from_mesh(pfg_solver *h)
+{
+    need(h->have_mesh, PFG_E_STATE, "setCRS before setDomain: no mesh");
+    build_pattern(h->mesh, h->K, h->st);
+    reset_system(h);
+}
+
+void ensure_crs(pfg_solver *h)
+{
+    if (!h->have_crs) set_crs_from_mesh(h);  // setValue calls setCRS itself (FEMSolverClass.f90:1015-1017)
+}
+
+KConfig to_config(const pfg_solve_opts *o)
+{
+    pfg_solve_opts d;
+    pfg_solve_opts_default(&d);
+    if (!o) o = &d;
+    KConfig c;
+    c.algorithm = o->algorithm;
+    c.precision = o->precision;
+    c.precond = o->precond;
+    c.stop_rule = o->stop_rule;
+    c.itrmax = o->itrmax;
+    c.er0 = o->er0;
+    c.relative_er = o->relative_er;
+    c.reliable_delta = o->reliable_delta;
+    c.graph_chunk = o->graph_chunk;
+    c.debug = o->debug;
+    return c;
+}
+
+void fill_info(pfg_info *info, const SolveResult &r, int precision)
+{
+    if (!info) return;
+    info->status = r.status;
+    info->iterations = r.iterations;
+    info->replacements = r.replacements;
+    info->kernel_launches = r.launches;
+    (void)precision;
+    info->rel_residual = r.rel_residual;
+    info->iter_residual = r.iter_residual;
+    info->solve_ms = r.ms;
+}
+
+int solve_status(const SolveResult &r)
+{
+    if (r.status == PFG_E_BREAKDOWN || r.status == PFG_E_NONFINITE) {
+        set_last_error(r.status == PFG_E_BREAKDOWN ? "Krylov breakdown (Bicgstab devide by zero)"
+                                                   : "non-finite value in a Krylov scalar");
+        return r.status;
+    }
+    if (r.status == PFG_W_NOT_CONVERGED) set_last_error("not converged within itrmax");
+    return r.status;
+}
+
+void apply_fix_device(pfg_solver *h)
+{
+    if (!h->have_fix) return;
+    const int64_t n = h->ndof();
+    h->fixed_d.ensure((size_t)n);
+    h->fixval_d.ensure((size_t)n);
+    PFG_CUDA(cudaMemcpyAsync(h->fixed_d.p, h->fixed_h.data(), n, cudaMemcpyHostToDevice, h->st));
+    PFG_CUDA(cudaMemcpyAsync(h->fixval_d.p, h->fixval_h.data(), n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    apply_dirichlet(h->K, h->rhs.p, h->fixed_d.p, h->fixval_d.p, h->st);
+}
+
+}  // namespace
+
+extern "C" {
+
+void pfg_solve_opts_default(pfg_solve_opts *o)
+{
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->algorithm = PFG_ALG_BICGSTAB;
+    o->precision = PFG_PREC_FP64;
+    o->precond = PFG_PC_NONE;
+    o->stop_rule = PFG_STOP_REFERENCE;
+    o->itrmax = 100000;
+    o->graph_chunk = 32;
+    o->er0 = 1.0e-10;
+    o->relative_er = 1.0e-10;
+    o->reliable_delta = 0.1;
+    o->debug = 0;
+}
+
+const char *pfg_last_error(void) { return g_last_error.c_str(); }
+const char *pfg_version(void) { return "plantfem_gb300 0.1 (sm_103a)"; }
+
+int pfg_create(pfg_solver **out)
+{
+    return guard([&] {
+        need(out != nullptr, PFG_E_ARG, "NULL handle pointer");
+        pfg_solver *h = new pfg_solver();
+        try {
+            PFG_CUDA(cudaGetDevice(&h->device));
+            PFG_CUDA(cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking));
+        } catch (...) {
+            delete h;
+            throw;
+        }
+        *out = h;
+    });
+}
+
+int pfg_destroy(pfg_solver *h)
+{
+    return guard([&] {
+        if (!h) return;
+        {
+            std::lock_guard<std::mutex> lk(h->mu);
+            cudaStreamSynchronize(h->st);
+        }
+        cudaStream_t st = h->st;
+        delete h;
+        if (st) cudaStreamDestroy(st);
+    });
+}
+
+int pfg_set_mesh(pfg_solver *h, int64_t nn, const double *nodcoord, int64_t ne, int32_t nne, const int32_t *elemnod)
+{
+    return guard([&] {
+        need(h && nodcoord && elemnod, PFG_E_ARG, "NULL argument");
+        need(nne == 8, PFG_E_UNSUPPORTED, "only 8-node hexahedra are supported");
+        need(nn > 0 && ne > 0 && nn < INT32_MAX, PFG_E_ARG, "bad mesh size");
+        std::lock_guard<std::mutex> lk(h->mu);
+        DevMesh &m = h->mesh;
+        m.nn = nn;
+        m.ne = ne;
+        m.conn_host.resize((size_t)ne * 8);
+        for (int64_t i = 0; i < ne * 8; ++i) {
+            const int32_t v = elemnod[i];
+            need(v >= 1 && v <= nn, PFG_E_ARG, "ElemNod entry out of range 1..nn");
+            m.conn_host[(size_t)i] = v - 1;
+        }
+        for (int64_t i = 0; i < nn * 3; ++i) need(std::isfinite(nodcoord[i]), PFG_E_NONFINITE, "non-finite NodCoord");
+        m.xyz.alloc((size_t)nn * 3);
+        m.conn.alloc((size_t)ne * 8);
+        PFG_CUDA(cudaMemcpyAsync(m.xyz.p, nodcoord, nn * 3 * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(m.conn.p, m.conn_host.data(), ne * 8 * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        color_elements(m, h->st);
+        h->have_mesh = true;
+        h->have_crs = false;
+    });
+}
+
+int pfg_set_crs(pfg_solver *h, int32_t dof)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        need(dof == 3, PFG_E_UNSUPPORTED, "setCRS: only DOF=3 (linear elasticity) is supported");
+        std::lock_guard<std::mutex> lk(h->mu);
+        set_crs_from_mesh(h);
+    });
+}
+
+int pfg_set_crs_arrays(pfg_solver *h, int64_t n, const int64_t *row_ptr, const int32_t *col_idx, const double *val)
+{
+    return guard([&] {
+        need(h && row_ptr && col_idx && val && n > 0, PFG_E_ARG, "bad CRS arguments");
+        need(row_ptr[0] == 1, PFG_E_ARG, "row_ptr(1) must be 1");
+        const int64_t nnz = row_ptr[n] - 1;
+        need(nnz >= 0, PFG_E_ARG, "row_ptr(n+1) < 1");
+        std::lock_guard<std::mutex> lk(h->mu);
+        DevBuf<int64_t> rp((size_t)n + 1);
+        DevBuf<int32_t> ci((size_t)std::max<int64_t>(nnz, 1));
+        DevBuf<double> v((size_t)std::max<int64_t>(nnz, 1));
+        PFG_CUDA(cudaMemcpyAsync(rp.p, row_ptr, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(ci.p, col_idx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(v.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        import_crs(n, nnz, rp.p, ci.p, v.p, h->K, h->st);
+        const bool keep_rhs = h->rhs.n >= (size_t)n && h->have_crs && h->ndof() == n;
+        if (!keep_rhs) reset_system(h);
+        h->have_crs = true;
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_get_crs_size(pfg_solver *h, int64_t *n, int64_t *nnz)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "no CRS matrix");
+        if (n) *n = h->ndof();
+        if (nnz) *nnz = h->K.nnzb * h->K.bs * h->K.bs;
+    });
+}
+
+int pfg_get_crs(pfg_solver *h, int64_t *row_ptr, int32_t *col_idx, double *val)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "no CRS matrix");
+        flush_pending(h);
+        const int64_t n = h->ndof(), nnz = h->K.nnzb * h->K.bs * h->K.bs;
+        DevBuf<int64_t> rp(row_ptr ? (size_t)n + 1 : 0);
+        DevBuf<int32_t> ci(col_idx ? (size_t)std::max<int64_t>(nnz, 1) : 0);
+        DevBuf<double> v(val ? (size_t)std::max<int64_t>(nnz, 1) : 0);
+        export_crs(h->K, rp.p, ci.p, v.p, h->st);
+        if (row_ptr) PFG_CUDA(cudaMemcpyAsync(row_ptr, rp.p, (n + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, h->st));
+        if (col_idx) PFG_CUDA(cudaMemcpyAsync(col_idx, ci.p, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost, h->st));
+        if (val) PFG_CUDA(cudaMemcpyAsync(val, v.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_set_rhs(pfg_solver *h, int64_t n, const double *rhs)
+{
+    return guard([&] {
+        need(h && rhs, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        ensure_crs(h);
+        need(n == h->ndof(), PFG_E_ARG, "setRHS: size differs from the CRS matrix");
+        PFG_CUDA(cudaMemcpyAsync(h->rhs.p, rhs, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_get_rhs(pfg_solver *h, int64_t n, double *rhs)
+{
+    return guard([&] {
+        need(h && rhs, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs && n == h->ndof(), PFG_E_ARG, "size differs from the CRS matrix");
+        flush_pending(h);
+        PFG_CUDA(cudaMemcpyAsync(rhs, h->rhs.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_set_matrix(pfg_solver *h, int32_t domain_id, int32_t element_id, int32_t dof, const double *matrix)
+{
+    if (domain_id != 1 || dof != 3) {
+        set_last_error("setMatrix: DomainID must be 1 and DOF 3");
+        return PFG_E_UNSUPPORTED;
+    }
+    return pfg_set_matrices(h, 1, &element_id, matrix);
+}
+
+int pfg_set_matrices(pfg_solver *h, int64_t count, const int32_t *element_ids, const double *matrices)
+{
+    return guard([&] {
+        need(h && element_ids && matrices && count >= 0, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "setMatrix before setDomain");
+        ensure_crs(h);
+        need(h->K.bs == 3, PFG_E_STATE, "setMatrix needs the mesh pattern (setCRS(DOF=3))");
+        for (int64_t i = 0; i < count; ++i) {
+            need(element_ids[i] >= 1 && element_ids[i] <= h->mesh.ne, PFG_E_ARG, "ElementID out of range");
+            h->pend_mat_ids.push_back(element_ids[i] - 1);
+        }
+        h->pend_mats.insert(h->pend_mats.end(), matrices, matrices + count * 576);
+        if (h->pend_mat_ids.size() >= 65536) flush_pending(h);
+    });
+}
+
+int pfg_set_vector(pfg_solver *h, int32_t domain_id, int32_t element_id, int32_t dof, const double *vector)
+{
+    return guard([&] {
+        need(h && vector, PFG_E_ARG, "NULL argument");
+        need(domain_id == 1 && dof == 3, PFG_E_UNSUPPORTED, "setVector: DomainID must be 1 and DOF 3");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "setVector before setDomain");
+        ensure_crs(h);
+        need(element_id >= 1 && element_id <= h->mesh.ne, PFG_E_ARG, "ElementID out of range");
+        h->pend_vec_ids.push_back(element_id - 1);
+        h->pend_vecs.insert(h->pend_vecs.end(), vector, vector + 24);
+        if (h->pend_vec_ids.size() >= 65536) flush_pending(h);
+    });
+}
+
+static void upload_prop(pfg_solver *h, int64_t n_prop, const double *p, DevBuf<double> &d, const char *name)
+{
+    need(p != nullptr, PFG_E_ARG, "NULL property array");
+    need(n_prop == 1 || n_prop == h->mesh.ne, PFG_E_ARG,
+         (std::string("size of ") + name + " should be 1 or number_of_element").c_str());
+    for (int64_t i = 0; i < n_prop; ++i) need(std::isfinite(p[i]), PFG_E_NONFINITE, "non-finite material property");
+    d.alloc((size_t)n_prop);
+    PFG_CUDA(cudaMemcpyAsync(d.p, p, n_prop * sizeof(double), cudaMemcpyHostToDevice, h->st));
+}
+
+int pfg_assemble_stiffness(pfg_solver *h, int64_t n_prop, const double *E, const double *nu)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "assemble before setDomain");
+        ensure_crs(h);
+        flush_pending(h);
+        DevBuf<double> dE, dnu;
+        upload_prop(h, n_prop, E, dE, "E");
+        upload_prop(h, n_prop, nu, dnu, "v");
+        assemble_elements(h->mesh, h->K, 0, dE.p, dnu.p, n_prop == 1, h->st);
+    });
+}
+
+int pfg_assemble_mass(pfg_solver *h, int64_t n_prop, const double *rho, int32_t lumped)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "assemble before setDomain");
+        ensure_crs(h);
+        flush_pending(h);
+        DevBuf<double> dr;
+        upload_prop(h, n_prop, rho, dr, "Density");
+        assemble_elements(h->mesh, h->K, lumped ? 2 : 1, dr.p, nullptr, n_prop == 1, h->st);
+    });
+}
+
+int pfg_assemble_body_force(pfg_solver *h, int64_t n_prop, const double *rho, const double accel[3])
+{
+    return guard([&] {
+        need(h && accel, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "assemble before setDomain");
+        ensure_crs(h);
+        flush_pending(h);
+        DevBuf<double> dr;
+        upload_prop(h, n_prop, rho, dr, "Density");
+        assemble_body_force(h->mesh, h->rhs.p, dr.p, n_prop == 1, accel, h->st);
+    });
+}
+
+int pfg_zeros(pfg_solver *h)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "zeros before setCRS");
+        h->pend_mat_ids.clear();
+        h->pend_mats.clear();
+        h->pend_vec_ids.clear();
+        h->pend_vecs.clear();
+        const int64_t nv = h->K.nnzb * h->K.bs * h->K.bs;
+        PFG_CUDA(cudaMemsetAsync(h->K.v64.p, 0, nv * sizeof(double), h->st));
+        PFG_CUDA(cudaMemsetAsync(h->rhs.p, 0, h->ndof() * sizeof(double), h->st));
+        h->K.v32_valid = false;
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_fix(pfg_solver *h, int64_t n, const int32_t *ids, const double *values, double value)
+{
+    return guard([&] {
+        need(h && (ids || n == 0), PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        ensure_crs(h);
+        const int64_t N = h->ndof();
+        for (int64_t i = 0; i < n; ++i) {
+            const int64_t id = ids[i];
+            if (id < 1 || id > N) continue;  // FEMSolverClass.f90:1106-1109
+            h->fixed_h[(size_t)id - 1] = 1;
+            h->fixval_h[(size_t)id - 1] = values ? values[i] : value;
+        }
+        h->have_fix = true;
+    });
+}
+
+int pfg_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *x0, double *x_out, pfg_info *info)
+{
+    SolveResult res;
+    const int rc = guard([&] {
+        need(h && x_out, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "solve before setCRS");
+        flush_pending(h);
+        const int64_t n = h->ndof();
+        apply_fix_device(h);
+        h->x.ensure((size_t)n);
+        if (x0)
+            PFG_CUDA(cudaMemcpyAsync(h->x.p, x0, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        else
+            PFG_CUDA(cudaMemsetAsync(h->x.p, 0, n * sizeof(double), h->st));
+        const KConfig cfg = to_config(opts);
+        res = h->kry.solve(h->K, h->rhs.p, h->x.p, cfg, h->st);
+        if (h->have_fix) restore_fixed(n, h->x.p, h->fixed_d.p, h->fixval_d.p, h->st);
+        PFG_CUDA(cudaMemcpyAsync(x_out, h->x.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        fill_info(info, res, cfg.precision);
+    });
+    if (rc != PFG_OK) return rc;
+    return solve_status(res);
+}
+
+int pfg_dev_spmv(pfg_solver *h, const double *d_x, double *d_y, void *stream)
+{
+    return guard([&] {
+        need(h && d_x && d_y, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "no CRS matrix");
+        flush_pending(h);
+        cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
+        if (st != h->st) PFG_CUDA(cudaStreamSynchronize(h->st));
+        Krylov::spmv64(h->K, d_x, d_y, st);
+        if (!stream) PFG_CUDA(cudaStreamSynchronize(st));  // own stream: done on return
+    });
+}
+
+int pfg_dev_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *d_b, double *d_x, pfg_info *info,
+                  void *stream)
+{
+    SolveResult res;
+    const int rc = guard([&] {
+        need(h && d_b && d_x, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "no CRS matrix");
+        flush_pending(h);
+        cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
+        if (st != h->st) PFG_CUDA(cudaStreamSynchronize(h->st));
+        const KConfig cfg = to_config(opts);
+        res = h->kry.solve(h->K, d_b, d_x, cfg, st);
+        fill_info(info, res, cfg.precision);
+    });
+    if (rc != PFG_OK) return rc;
+    return solve_status(res);
+}
+
+// ------------------------------------------------------ reference plug-ins
+}  // extern "C"
+
+namespace {
+
+template <typename T>
+int crs_spmv_host(const T *val, const int64_t *row_ptr, const int32_t *col_idx, const T *old_vector, T *new_vector,
+                  size_t n, size_t col_size)
+{
+    return guard([&] {
+        need(val && row_ptr && col_idx && old_vector && new_vector, PFG_E_ARG, "NULL argument");
+        if (n == 0) return;
+        need(row_ptr[0] == 1, PFG_E_ARG, "row_ptr(1) must be 1");
+        const int64_t nnz = row_ptr[n] - 1;
+        need(nnz >= 0 && (size_t)nnz <= col_size, PFG_E_ARG, "row_ptr(n+1)-1 exceeds col_size");
+        cudaStream_t st;
+        PFG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() { cudaStreamDestroy(s); }
+        } sg{st};
+        DevBuf<int64_t> rp(n + 1);
+        DevBuf<int32_t> ci((size_t)std::max<int64_t>(nnz, 1));
+        DevBuf<T> x(n), y(n);
+        PFG_CUDA(cudaMemcpyAsync(rp.p, row_ptr, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        PFG_CUDA(cudaMemcpyAsync(ci.p, col_idx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        PFG_CUDA(cudaMemcpyAsync(x.p, old_vector, n * sizeof(T), cudaMemcpyHostToDevice, st));
+        // Scalar rows (1x1 blocks, one warp per row): the reference's operator
+        // exactly, whatever its structure.
+        DevMatrix A;
+        import_crs((int64_t)n, nnz, rp.p, ci.p, nullptr, A, st, /*allow_blocks=*/false);
+        if (sizeof(T) == 8) {
+            PFG_CUDA(cudaMemcpyAsync(A.v64.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, st));
+            Krylov::spmv64(A, (const double *)x.p, (double *)y.p, st);
+        } else {
+            A.v32.alloc((size_t)std::max<int64_t>(nnz, 1));
+            PFG_CUDA(cudaMemcpyAsync(A.v32.p, val, nnz * sizeof(float), cudaMemcpyHostToDevice, st));
+            A.v32_valid = true;
+            Krylov::spmv32(A, (const float *)x.p, (float *)y.p, st);
+        }
+        std::vector<T> hy(n);
+        PFG_CUDA(cudaMemcpyAsync(hy.data(), y.p, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+        PFG_CUDA(cudaStreamSynchronize(st));
+        // SparseClass-c.c:139-141 accumulates into new_vector
+        for (size_t i = 0; i < n; ++i) new_vector[i] = new_vector[i] + hy[i];
+    });
+}
+
+}  // namespace
+
+extern "C" {
+
+int pfg_crs_spmv_real64(const double *val, const int64_t *row_ptr, const int32_t *col_idx, const double *old_vector,
+                        double *new_vector, size_t n, size_t col_size)
+{
+    return crs_spmv_host<double>(val, row_ptr, col_idx, old_vector, new_vector, n, col_size);
+}
+
+int pfg_crs_spmv_real32(const float *val, const int64_t *row_ptr, const int32_t *col_idx, const float *old_vector,
+                        float *new_vector, size_t n, size_t col_size)
+{
+    return crs_spmv_host<float>(val, row_ptr, col_idx, old_vector, new_vector, n, col_size);
+}
+
+int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const double *val, const double *rhs,
+                          double *x, int64_t n, int64_t nnz, const pfg_solve_opts *opts, pfg_info *info)
+{
+    // One cached context per thread: device buffers and captured graphs are
+    // reused when the same-size system is solved again.
+    static thread_local pfg_solver *ctx = nullptr;
+    SolveResult res;
+    const int rc = guard([&] {
+        need(row_ptr && col_idx && val && rhs && x && n > 0, PFG_E_ARG, "NULL argument");
+        need(row_ptr[0] == 1 && row_ptr[n] - 1 == nnz, PFG_E_ARG, "row_ptr inconsistent with nnz");
+        if (!ctx) {
+            pfg_solver *h = nullptr;
+            if (pfg_create(&h) != PFG_OK) throw Error(PFG_E_CUDA, pfg_last_error());
+            ctx = h;
+        }
+        pfg_solver *h = ctx;
+        std::lock_guard<std::mutex> lk(h->mu);
+        static thread_local DevBuf<int64_t> rp;
+        static thread_local DevBuf<int32_t> ci;
+        static thread_local DevBuf<double> v, b;
+        rp.ensure((size_t)n + 1);
+        ci.ensure((size_t)std::max<int64_t>(nnz, 1));
+        v.ensure((size_t)std::max<int64_t>(nnz, 1));
+        b.ensure((size_t)n);
+        PFG_CUDA(cudaMemcpyAsync(rp.p, row_ptr, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(ci.p, col_idx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(v.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaMemcpyAsync(b.p, rhs, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        const bool same = h->have_crs && h->ndof() == n && h->K.nnzb * h->K.bs * h->K.bs == nnz;
+        if (same) {
+            // same structure as last time: re-import values into the existing buffers
+            DevMatrix tmp;
+            import_crs(n, nnz, rp.p, ci.p, v.p, tmp, h->st);
+            if (tmp.bs == h->K.bs) {
+                std::swap(h->K.rp, tmp.rp);
+                std::swap(h->K.col, tmp.col);
+                std::swap(h->K.v64, tmp.v64);
+                h->K.v32_valid = false;
+            } else {
+                h->K = std::move(tmp);
+            }
+        } else {
+            import_crs(n, nnz, rp.p, ci.p, v.p, h->K, h->st);
+            h->have_crs = true;
+        }
+        h->x.ensure((size_t)n);
+        PFG_CUDA(cudaMemcpyAsync(h->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        const KConfig cfg = to_config(opts);
+        res = h->kry.solve(h->K, b.p, h->x.p, cfg, h->st);
+        PFG_CUDA(cudaMemcpyAsync(x, h->x.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        fill_info(info, res, cfg.precision);
+    });
+    if (rc != PFG_OK) return rc;
+    return solve_status(res);
+}
+
+}  // extern "C"
+
+extern "C" int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, double *ms_per_launch,
+                                  double *bytes_per_launch)
+{
+    return guard([&] {
+        need(h && ms_per_launch && bytes_per_launch, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "no CRS matrix");
+        flush_pending(h);
+        h->kry.profile(h->K, kernel, reps, h->st, *ms_per_launch, *bytes_per_launch);
+    });
+}

@@ -1,0 +1,1220 @@
+// krylov.cu -- CG and BiCGSTAB on the device, FP64 and mixed precision.
+//
+// Restates bicgstab_CRS_2 (FEMSolverClass.f90:2199-2298) and adds CG for the
+// symmetric eliminated system.  Design:
+//   * every scalar (rho, alpha, beta, c1..c3, norms) lives in device memory
+//     (KState); the last CTA of each fused reduction computes the next scalars,
+//     so one iteration is 2 (CG) or 3 (BiCGSTAB) kernel launches and no host
+//     round trip;
+//   * the direction update p = z + beta p (CG) or p = r + beta (p - c3 y)
+//     (BiCGSTAB) is fused into the SpMV that consumes p: the gathered source
+//     value of every block column is formed on the fly, the owning warp writes
+//     the row's new p to a ping-pong buffer;
+//   * a chunk of iterations is captured once into a CUDA graph and replayed;
+//     kernels return at entry once KState says done (or, mixed precision, that
+//     a residual replacement is due), and the host checks KState once per chunk;
+//   * mixed precision: matrix, vectors and dots in FP32 (dots compensated,
+//     Dot2 of Ogita-Rump-Oishi); the solution is accumulated in FP64 and the
+//     FP32 residual is replaced by the FP64 residual b - A x (FP64 SpMV) each
+//     time it dropped by reliable_delta ("reliable updates", Sleijpen & van der
+//     Vorst 1996, as used for mixed-precision CG by Clark et al. 2010).  The
+//     stop test is always on that FP64 residual.
+#include <cmath>
+
+#include "krylov.cuh"
+
+namespace pfg {
+
+static int g_sm_count = 0;
+
+static int sm_count()
+{
+    if (g_sm_count == 0) {
+        int dev = 0;
+        PFG_CUDA(cudaGetDevice(&dev));
+        PFG_CUDA(cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev));
+        if (g_sm_count <= 0) g_sm_count = 1;
+    }
+    return g_sm_count;
+}
+
+constexpr int kThreads = 256;  // 8 warps per CTA for every row kernel
+constexpr int kWarps = kThreads / 32;
+
+int Krylov::row_grid(int64_t nb)
+{
+    // Persistent-style grid: a fixed number of resident CTAs per SM, each warp
+    // striding over block rows.  6 CTAs x 256 threads keeps 48 warps per SM.
+    int64_t want = (nb + kWarps - 1) / kWarps;
+    int64_t cap = (int64_t)sm_count() * 6;
+    return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+template <int BS, typename T>
+__device__ __forceinline__ T pick(const T (&y)[BS], int i)
+{
+    T v = y[0];
+#pragma unroll
+    for (int k = 1; k < BS; ++k) v = (i == k) ? y[k] : v;
+    return v;
+}
+
+// ---------------------------------------------------------------- reductions
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+    using type = double;
+    __device__ static double zero() { return 0.0; }
+    __device__ static void add(double &a, double x, double y) { a = fma(x, y, a); }
+};
+template <>
+struct Acc<float> {
+    using type = Comp32;
+    __device__ static Comp32 zero() { return Comp32{0.f, 0.f}; }
+    __device__ static void add(Comp32 &a, float x, float y) { comp_add_prod(a, x, y); }
+};
+
+template <int NV>
+__device__ __forceinline__ bool grid_total(double (&v)[NV], double *pd, float *, unsigned *ticket,
+                                           double (&tot)[NV])
+{
+    return grid_sum<NV>(v, pd, ticket, tot);
+}
+template <int NV>
+__device__ __forceinline__ bool grid_total(Comp32 (&v)[NV], double *, float *pf, unsigned *ticket,
+                                           float (&tot)[NV])
+{
+    return grid_sum_comp<NV>(v, pf, ticket, tot);
+}
+
+__device__ __forceinline__ bool finite_d(double x) { return isfinite(x); }
+
+// ------------------------------------------------------------ plain kernels
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads) k_spmv(BsrView<T> A, const T *__restrict__ x, T *__restrict__ y)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t row = w0; row < A.nb; row += nw) {
+        T acc[BS];
+        auto src = [&](int c, T(&xv)[BS]) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) xv[i] = __ldg(x + (int64_t)BS * c + i);
+        };
+        bsr_row_product<BS>(A, row, lane, src, acc);
+        if (lane < BS) y[(int64_t)BS * row + lane] = pick<BS>(acc, lane);
+    }
+}
+
+// r = b - A x in FP64; totals: rr = r.r and bb = b.b; stores into KState
+// (true_rr, bb) or, when mode==1, into rr/rr1 as the initial recursive residual.
+template <int BS>
+__global__ void __launch_bounds__(kThreads) k_residual64(BsrView<double> A, const double *__restrict__ b,
+                                                         const double *__restrict__ x, double *__restrict__ r,
+                                                         KState *S, double *partials, unsigned *ticket)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    double acc[2] = {0.0, 0.0};
+    for (int64_t row = w0; row < A.nb; row += nw) {
+        double y[BS];
+        auto src = [&](int c, double(&xv)[BS]) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) xv[i] = __ldg(x + (int64_t)BS * c + i);
+        };
+        bsr_row_product<BS>(A, row, lane, src, y);
+        if (lane < BS) {
+            const int64_t i = (int64_t)BS * row + lane;
+            const double bi = b[i];
+            const double ri = bi - pick<BS>(y, lane);
+            r[i] = ri;
+            acc[0] = fma(ri, ri, acc[0]);
+            acc[1] = fma(bi, bi, acc[1]);
+        }
+    }
+    double tot[2];
+    if (grid_sum<2>(acc, partials, ticket, tot)) {
+        S->true_rr = tot[0];
+        S->bb = tot[1];
+    }
+}
+
+template <int BS, typename T>
+__device__ __forceinline__ void pc_apply(int pc, const T *__restrict__ dinv, int64_t row, const T (&r)[BS],
+                                         T (&z)[BS])
+{
+    if (pc == PFG_PC_NONE) {
+#pragma unroll
+        for (int i = 0; i < BS; ++i) z[i] = r[i];
+        return;
+    }
+    const T *D = dinv + row * (BS * BS);
+#pragma unroll
+    for (int i = 0; i < BS; ++i) {
+        T s = T(0);
+#pragma unroll
+        for (int j = 0; j < BS; ++j) s = fma(__ldg(D + i * BS + j), r[j], s);
+        z[i] = s;
+    }
+}
+
+// Inverse of the diagonal block of every block row (block Jacobi), or of the
+// diagonal entries only (point Jacobi).  A zero pivot keeps the identity, as
+// JacobiPreconditionerCRS skips rows with A_kk == 0 (FEMSolverClass.f90:2519).
+template <int BS>
+__global__ void k_precond(BsrView<double> A, int pc, double *__restrict__ d64, float *__restrict__ d32)
+{
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < A.nb;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = A.rp[row];
+        const int nblk = (int)(A.rp[row + 1] - s);
+        double D[BS * BS];
+#pragma unroll
+        for (int e = 0; e < BS * BS; ++e) D[e] = 0.0;
+        for (int k = 0; k < nblk; ++k)
+            if (A.col[s + k] == row) {
+#pragma unroll
+                for (int e = 0; e < BS * BS; ++e) D[e] = A.val[s * BS * BS + (int64_t)e * nblk + k];
+                break;
+            }
+        double Inv[BS * BS];
+#pragma unroll
+        for (int e = 0; e < BS * BS; ++e) Inv[e] = 0.0;
+        if (pc == PFG_PC_JACOBI || BS == 1) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) Inv[i * BS + i] = D[i * BS + i] != 0.0 ? 1.0 / D[i * BS + i] : 1.0;
+        } else {
+            // 3x3 inverse by cofactors
+            const double a = D[0], b = D[1], c = D[2], d = D[3], e = D[4], f = D[5], g = D[6], h = D[7],
+                         k = D[8];
+            const double c0 = e * k - f * h, c1 = f * g - d * k, c2 = d * h - e * g;
+            const double det = a * c0 + b * c1 + c * c2;
+            if (det != 0.0 && isfinite(det)) {
+                const double id = 1.0 / det;
+                Inv[0] = c0 * id;
+                Inv[1] = (c * h - b * k) * id;
+                Inv[2] = (b * f - c * e) * id;
+                Inv[3] = c1 * id;
+                Inv[4] = (a * k - c * g) * id;
+                Inv[5] = (c * d - a * f) * id;
+                Inv[6] = c2 * id;
+                Inv[7] = (b * g - a * h) * id;
+                Inv[8] = (a * e - b * d) * id;
+            } else {
+#pragma unroll
+                for (int i = 0; i < BS; ++i) Inv[i * BS + i] = D[i * BS + i] != 0.0 ? 1.0 / D[i * BS + i] : 1.0;
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < BS * BS; ++e) {
+            d64[row * BS * BS + e] = Inv[e];
+            if (d32) d32[row * BS * BS + e] = (float)Inv[e];
+        }
+    }
+}
+
+__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+// ------------------------------------------------------------------ CG kernels
+template <typename T>
+__device__ __forceinline__ T st_beta(const KState *S);
+template <>
+__device__ __forceinline__ double st_beta<double>(const KState *S) { return S->beta; }
+template <>
+__device__ __forceinline__ float st_beta<float>(const KState *S) { return S->beta32; }
+template <typename T>
+__device__ __forceinline__ T st_alpha(const KState *S);
+template <>
+__device__ __forceinline__ double st_alpha<double>(const KState *S) { return S->alpha; }
+template <>
+__device__ __forceinline__ float st_alpha<float>(const KState *S) { return S->alpha32; }
+
+// q = A p_new, p_new = z + beta p_old formed on the fly; pq = p_new . q;
+// fin: alpha = rho / pq.
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_spmv(BsrView<T> A, const T *__restrict__ z, T *pA, T *pB, T *__restrict__ q, KState *S, double *pd,
+              float *pf, unsigned *ticket)
+{
+    if (S->done | S->need_update) return;
+    const T beta = st_beta<T>(S);
+    const int par = S->parity;
+    const T *pold = par ? pB : pA;
+    T *pnew = par ? pA : pB;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    typename Acc<T>::type acc[1] = {Acc<T>::zero()};
+    for (int64_t row = w0; row < A.nb; row += nw) {
+        T y[BS];
+        auto src = [&](int c, T(&xv)[BS]) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) {
+                const int64_t j = (int64_t)BS * c + i;
+                xv[i] = fma(beta, __ldg(pold + j), __ldg(z + j));
+            }
+        };
+        bsr_row_product<BS>(A, row, lane, src, y);
+        if (lane < BS) {
+            const int64_t i = (int64_t)BS * row + lane;
+            const T pn = fma(beta, pold[i], z[i]);
+            const T qi = pick<BS>(y, lane);
+            pnew[i] = pn;
+            q[i] = qi;
+            Acc<T>::add(acc[0], pn, qi);
+        }
+    }
+    T tot[1];
+    if (grid_total<1>(acc, pd, pf, ticket, tot)) {
+        const double pq = (double)tot[0];
+        if (!(pq > 0.0) || !finite_d(pq)) {
+            S->status = PFG_E_BREAKDOWN;
+            S->done = 1;
+        } else if (sizeof(T) == 8) {
+            S->pq = pq;
+            S->alpha = S->rho / pq;
+        } else {
+            S->alpha32 = (float)(S->rho32 / tot[0]);
+        }
+    }
+}
+
+// x += alpha p_new; r -= alpha q; z = M^-1 r; rho' = r.z; rr = r.r.
+// fin (FP64): beta = rho'/rho, stop test on the recursive residual.
+// fin (FP32): same, or request a residual replacement.
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_update(int64_t nb, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *pA, const T *pB,
+                const T *__restrict__ q, const T *__restrict__ dinv, int pc, KState *S, double *pd, float *pf,
+                unsigned *ticket, double tol, double delta, int itrmax)
+{
+    if (S->done | S->need_update) return;
+    const T alpha = st_alpha<T>(S);
+    const T *pnew = S->parity ? pA : pB;
+    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        T rv[BS], zv[BS];
+#pragma unroll
+        for (int i = 0; i < BS; ++i) {
+            const int64_t j = (int64_t)BS * row + i;
+            x[j] = fma(alpha, pnew[j], x[j]);
+            rv[i] = fma(-alpha, q[j], r[j]);
+            r[j] = rv[i];
+        }
+        pc_apply<BS, T>(pc, dinv, row, rv, zv);
+#pragma unroll
+        for (int i = 0; i < BS; ++i) {
+            z[(int64_t)BS * row + i] = zv[i];
+            Acc<T>::add(acc[0], rv[i], zv[i]);
+            Acc<T>::add(acc[1], rv[i], rv[i]);
+        }
+    }
+    T tot[2];
+    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+        S->iter += 1;
+        S->parity ^= 1;
+        const double rho_n = (double)tot[0], rr = (double)tot[1];
+        if (!finite_d(rho_n) || !finite_d(rr)) {
+            S->status = PFG_E_NONFINITE;
+            S->done = 1;
+            return;
+        }
+        if (sizeof(T) == 8) {
+            S->rr = rr;
+            S->beta = rho_n / S->rho;
+            S->rho = rho_n;
+            if (sqrt(rr) <= tol * sqrt(S->bb)) S->done = 1;
+        } else {
+            const float rn = sqrtf((float)rr);
+            S->rr32 = (float)rr;
+            S->rmax32 = fmaxf(S->rmax32, rn);
+            if ((double)rn < delta * (double)S->rmax32 || (double)rn <= tol * sqrt(S->bb)) {
+                S->need_update = 1;  // replacement recomputes rho and beta
+            } else {
+                S->beta32 = (float)(rho_n / (double)S->rho32);
+                S->rho32 = (float)rho_n;
+            }
+        }
+        if (S->iter >= itrmax && !S->done) {
+            S->status = PFG_W_NOT_CONVERGED;
+            S->done = 1;
+        }
+    }
+}
+
+// (Re)start of CG from the residual r: z = M^-1 r, rho = r.z, beta = 0.
+// FP32 version also folds in the residual replacement bookkeeping.
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_restart(int64_t nb, const T *__restrict__ r, T *__restrict__ z, const T *__restrict__ dinv, int pc,
+                 KState *S, double *pd, float *pf, unsigned *ticket, int keep_direction)
+{
+    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        T rv[BS], zv[BS];
+#pragma unroll
+        for (int i = 0; i < BS; ++i) rv[i] = r[(int64_t)BS * row + i];
+        pc_apply<BS, T>(pc, dinv, row, rv, zv);
+#pragma unroll
+        for (int i = 0; i < BS; ++i) {
+            z[(int64_t)BS * row + i] = zv[i];
+            Acc<T>::add(acc[0], rv[i], zv[i]);
+            Acc<T>::add(acc[1], rv[i], rv[i]);
+        }
+    }
+    T tot[2];
+    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+        if (sizeof(T) == 8) {
+            S->rho = (double)tot[0];
+            S->rr = (double)tot[1];
+            S->beta = 0.0;
+        } else {
+            const float rho_n = tot[0];
+            S->beta32 = (keep_direction && S->rho32 != 0.f) ? rho_n / S->rho32 : 0.f;
+            S->rho32 = rho_n;
+            S->rr32 = tot[1];
+            S->rmax32 = sqrtf(tot[1]);
+            S->need_update = 0;
+        }
+    }
+}
+
+// ------------------------------------------------------------ BiCGSTAB kernels
+// y_new = A p_new, p_new = r + beta (p_old - c3 y_old) on the fly; c2 = r0.y_new;
+// fin: alpha = c1 / c2  (FEMSolverClass.f90:2236-2248, 2296).
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_bicg_spmv1(BsrView<T> A, const T *__restrict__ r, const T *__restrict__ r0, T *pA, T *pB, T *yA, T *yB,
+                 KState *S, double *pd, float *pf, unsigned *ticket)
+{
+    if (S->done | S->need_update) return;
+    const bool f64 = sizeof(T) == 8;
+    const T beta = f64 ? (T)S->beta : (T)S->beta32;
+    const T c3 = f64 ? (T)S->c3 : (T)S->c3_32;
+    const int par = S->parity;
+    const T *pold = par ? pB : pA;
+    T *pnew = par ? pA : pB;
+    const T *yold = par ? yB : yA;
+    T *ynew = par ? yA : yB;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    typename Acc<T>::type acc[1] = {Acc<T>::zero()};
+    for (int64_t row = w0; row < A.nb; row += nw) {
+        T y[BS];
+        auto src = [&](int c, T(&xv)[BS]) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) {
+                const int64_t j = (int64_t)BS * c + i;
+                xv[i] = fma(beta, fma(-c3, __ldg(yold + j), __ldg(pold + j)), __ldg(r + j));
+            }
+        };
+        bsr_row_product<BS>(A, row, lane, src, y);
+        if (lane < BS) {
+            const int64_t i = (int64_t)BS * row + lane;
+            const T pn = fma(beta, fma(-c3, yold[i], pold[i]), r[i]);
+            const T yi = pick<BS>(y, lane);
+            pnew[i] = pn;
+            ynew[i] = yi;
+            Acc<T>::add(acc[0], r0[i], yi);
+        }
+    }
+    T tot[1];
+    if (grid_total<1>(acc, pd, pf, ticket, tot)) {
+        const double c2 = (double)tot[0];
+        if (c2 == 0.0 || !finite_d(c2)) {
+            S->status = PFG_E_BREAKDOWN;
+            S->done = 1;
+        } else if (f64) {
+            S->c2 = c2;
+            S->alpha = S->c1 / c2;
+        } else {
+            S->c2_32 = tot[0];
+            S->alpha32 = S->c1_32 / tot[0];
+        }
+    }
+}
+
+// v = A e, e = r - alpha y_new on the fly; ev = e.v, vv = v.v; fin: c3 = ev/vv
+// (FEMSolverClass.f90:2254-2267).
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_bicg_spmv2(BsrView<T> A, const T *__restrict__ r, const T *yA, const T *yB, T *__restrict__ e,
+                 T *__restrict__ v, KState *S, double *pd, float *pf, unsigned *ticket)
+{
+    if (S->done | S->need_update) return;
+    const bool f64 = sizeof(T) == 8;
+    const T alpha = f64 ? (T)S->alpha : (T)S->alpha32;
+    const T *ynew = S->parity ? yA : yB;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    for (int64_t row = w0; row < A.nb; row += nw) {
+        T y[BS];
+        auto src = [&](int c, T(&xv)[BS]) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) {
+                const int64_t j = (int64_t)BS * c + i;
+                xv[i] = fma(-alpha, __ldg(ynew + j), __ldg(r + j));
+            }
+        };
+        bsr_row_product<BS>(A, row, lane, src, y);
+        if (lane < BS) {
+            const int64_t i = (int64_t)BS * row + lane;
+            const T ei = fma(-alpha, ynew[i], r[i]);
+            const T vi = pick<BS>(y, lane);
+            e[i] = ei;
+            v[i] = vi;
+            Acc<T>::add(acc[0], ei, vi);
+            Acc<T>::add(acc[1], vi, vi);
+        }
+    }
+    T tot[2];
+    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+        const double vv = (double)tot[1];
+        if (vv == 0.0 || !finite_d(vv) || !finite_d((double)tot[0])) {
+            S->status = PFG_E_BREAKDOWN;
+            S->done = 1;
+        } else if (f64) {
+            S->ev = (double)tot[0];
+            S->vv = vv;
+            S->c3 = (double)tot[0] / vv;
+        } else {
+            S->c3_32 = tot[0] / tot[1];
+        }
+    }
+}
+
+// x += alpha p_new + c3 e; r = e - c3 v; rr = r.r; c1' = r0.r; stop rules and
+// beta = c1' / (c2 c3) (FEMSolverClass.f90:2268-2296).
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_bicg_update(int64_t nb, T *__restrict__ x, T *__restrict__ r, const T *__restrict__ r0, const T *pA,
+                  const T *pB, const T *__restrict__ e, const T *__restrict__ v, KState *S, double *pd, float *pf,
+                  unsigned *ticket, int stop_rule, double er0, double tol, double delta, int itrmax)
+{
+    if (S->done | S->need_update) return;
+    const bool f64 = sizeof(T) == 8;
+    const T alpha = f64 ? (T)S->alpha : (T)S->alpha32;
+    const T c3 = f64 ? (T)S->c3 : (T)S->c3_32;
+    const T *pnew = S->parity ? pA : pB;
+    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    const int64_t n = nb * BS;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T ei = e[i];
+        x[i] = x[i] + alpha * pnew[i] + c3 * ei;
+        const T ri = fma(-c3, v[i], ei);
+        r[i] = ri;
+        Acc<T>::add(acc[0], ri, ri);
+        Acc<T>::add(acc[1], r0[i], ri);
+    }
+    T tot[2];
+    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+        S->iter += 1;
+        S->parity ^= 1;
+        const double rr = (double)tot[0], c1n = (double)tot[1];
+        if (!finite_d(rr) || !finite_d(c1n)) {
+            S->status = PFG_E_NONFINITE;
+            S->done = 1;
+            return;
+        }
+        if (f64) {
+            S->rr = rr;
+            if (S->iter == 1) S->rr1 = rr;
+            bool stop;
+            if (stop_rule == PFG_STOP_REFERENCE)
+                stop = (sqrt(rr / S->rr1) < tol) || (sqrt(rr) < er0);
+            else
+                stop = sqrt(rr) <= tol * sqrt(S->bb);
+            if (stop) {
+                S->done = 1;
+            } else {
+                const double c2c3 = S->c2 * S->c3;
+                if (c2c3 == 0.0) {
+                    S->status = PFG_E_BREAKDOWN;
+                    S->done = 1;
+                } else {
+                    S->beta = c1n / c2c3;
+                    S->c1 = c1n;
+                }
+            }
+        } else {
+            const float rn = sqrtf((float)rr);
+            S->rr32 = (float)rr;
+            S->rmax32 = fmaxf(S->rmax32, rn);
+            if ((double)rn < delta * (double)S->rmax32 || (double)rn <= tol * sqrt(S->bb)) {
+                S->need_update = 1;
+            } else {
+                const float c2c3 = S->c2_32 * S->c3_32;
+                if (c2c3 == 0.f) {
+                    S->status = PFG_E_BREAKDOWN;
+                    S->done = 1;
+                } else {
+                    S->beta32 = (float)c1n / c2c3;
+                    S->c1_32 = (float)c1n;
+                }
+            }
+        }
+        if (S->iter >= itrmax && !S->done) {
+            S->status = PFG_W_NOT_CONVERGED;
+            S->done = 1;
+        }
+    }
+}
+
+// BiCGSTAB (re)start from r: r0 = r (first start only), c1 = r0.r, beta = 0.
+// keep_direction != 0 (mixed replacement): keep p, y and r0, beta = c1'/(c2 c3).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_bicg_restart(int64_t n, const T *__restrict__ r, T *__restrict__ r0, KState *S, double *pd, float *pf,
+                   unsigned *ticket, int set_r0, int keep_direction)
+{
+    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const T ri = r[i];
+        if (set_r0) r0[i] = ri;
+        const T r0i = set_r0 ? ri : r0[i];
+        Acc<T>::add(acc[0], r0i, ri);
+        Acc<T>::add(acc[1], ri, ri);
+    }
+    T tot[2];
+    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+        if (sizeof(T) == 8) {
+            S->c1 = (double)tot[0];
+            S->rr = (double)tot[1];
+            S->beta = 0.0;
+            S->c3 = 0.0;
+        } else {
+            const float c1n = tot[0];
+            const float c2c3 = S->c2_32 * S->c3_32;
+            S->beta32 = (keep_direction && c2c3 != 0.f) ? c1n / c2c3 : 0.f;
+            if (!keep_direction) S->c3_32 = 0.f;
+            S->c1_32 = c1n;
+            S->rr32 = tot[1];
+            S->rmax32 = sqrtf(tot[1]);
+            S->need_update = 0;
+        }
+    }
+}
+
+// --------------------------------------------------- mixed-precision plumbing
+// x64 += x32, x32 = 0 (fold the FP32 correction into the FP64 solution).
+__global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ x32)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x64[i] += (double)x32[i];
+        x32[i] = 0.f;
+    }
+}
+
+// r32 = (float) r64 after the FP64 residual; decides convergence on it.
+__global__ void k_replace(int64_t n, const double *__restrict__ r64, float *__restrict__ r32, KState *S,
+                          double tol)
+{
+    const bool conv = sqrt(S->true_rr) <= tol * sqrt(S->bb);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r32[i] = (float)r64[i];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        S->replacements += 1;
+        if (conv) S->done = 1;
+    }
+}
+
+// ------------------------------------------------------------------- host side
+Krylov::Krylov()
+{
+    PFG_CUDA(cudaMallocHost((void **)&host_state_, sizeof(KState)));
+    memset(host_state_, 0, sizeof(KState));
+}
+
+Krylov::~Krylov()
+{
+    if (graph_) cudaGraphExecDestroy(graph_);
+    if (host_state_) cudaFreeHost(host_state_);
+}
+
+template <int BS, typename T>
+static void launch_spmv(const DevMatrix &A, BsrView<T> v, const T *x, T *y, cudaStream_t st)
+{
+    if (A.nb == 0) return;
+    k_spmv<BS, T><<<Krylov::row_grid(A.nb), kThreads, 0, st>>>(v, x, y);
+    PFG_CUDA(cudaGetLastError());
+}
+
+void Krylov::spmv64(const DevMatrix &A, const double *x, double *y, cudaStream_t st)
+{
+    if (A.bs == 3)
+        launch_spmv<3, double>(A, A.view<double>(), x, y, st);
+    else
+        launch_spmv<1, double>(A, A.view<double>(), x, y, st);
+}
+
+void Krylov::spmv32(const DevMatrix &A, const float *x, float *y, cudaStream_t st)
+{
+    PFG_CHECK(A.v32_valid, PFG_E_STATE, "FP32 matrix copy not built");
+    if (A.bs == 3)
+        launch_spmv<3, float>(A, A.view<float>(), x, y, st);
+    else
+        launch_spmv<1, float>(A, A.view<float>(), x, y, st);
+}
+
+void Krylov::make_v32(DevMatrix &A, cudaStream_t st)
+{
+    const int64_t nv = A.nnzb * A.bs * A.bs;
+    A.v32.ensure((size_t)std::max<int64_t>(nv, 1));
+    if (nv) {
+        k_to_f32<<<grid_for(nv, 256, sm_count() * 8), 256, 0, st>>>(A.v64.p, A.v32.p, nv);
+        PFG_CUDA(cudaGetLastError());
+    }
+    A.v32_valid = true;
+}
+
+void Krylov::prepare(const DevMatrix &A, const KConfig &cfg, cudaStream_t st)
+{
+    const int64_t n = A.ndof();
+    const bool mixed = cfg.precision == PFG_PREC_MIXED;
+    n_ = n;
+    bs_ = A.bs;
+    const size_t nn = (size_t)std::max<int64_t>(n, 1);
+    r_.ensure(nn);
+    z_.ensure(nn);
+    pA_.ensure(nn);
+    pB_.ensure(nn);
+    q_.ensure(nn);
+    if (!mixed && cfg.algorithm == PFG_ALG_BICGSTAB) {
+        r0_.ensure(nn);
+        yA_.ensure(nn);
+        yB_.ensure(nn);
+        e_.ensure(nn);
+        v_.ensure(nn);
+    }
+    if (mixed) {
+        r32_.ensure(nn);
+        z32_.ensure(nn);
+        pA32_.ensure(nn);
+        pB32_.ensure(nn);
+        q32_.ensure(nn);
+        x32_.ensure(nn);
+        if (cfg.algorithm == PFG_ALG_BICGSTAB) {
+            r032_.ensure(nn);
+            yA32_.ensure(nn);
+            yB32_.ensure(nn);
+            e32_.ensure(nn);
+            v32_.ensure(nn);
+        }
+    }
+    const int g = row_grid(A.nb);
+    partials_.ensure((size_t)g * 4 + 8);
+    partials32_.ensure((size_t)g * 8 + 16);
+    if (!ticket_.p) {
+        ticket_.alloc(1);
+        PFG_CUDA(cudaMemsetAsync(ticket_.p, 0, sizeof(unsigned), st));
+    }
+    if (!state_.p) state_.alloc(1);
+    PFG_CUDA(cudaMemsetAsync(state_.p, 0, sizeof(KState), st));
+    (void)st;
+}
+
+void Krylov::build_precond(const DevMatrix &A, int precond, bool fp32, cudaStream_t st)
+{
+    if (precond == PFG_PC_NONE) return;
+    const size_t m = (size_t)std::max<int64_t>(A.nb * A.bs * A.bs, 1);
+    dinv_.ensure(m);
+    if (fp32) dinv32_.ensure(m);
+    const int g = grid_for(A.nb, 256, sm_count() * 8);
+    if (A.bs == 3)
+        k_precond<3><<<g, 256, 0, st>>>(A.view<double>(), precond, dinv_.p, fp32 ? dinv32_.p : nullptr);
+    else
+        k_precond<1><<<g, 256, 0, st>>>(A.view<double>(), precond, dinv_.p, fp32 ? dinv32_.p : nullptr);
+    PFG_CUDA(cudaGetLastError());
+    ++launches_;
+}
+
+void Krylov::read_state(KState &h, cudaStream_t st)
+{
+    PFG_CUDA(cudaMemcpyAsync(host_state_, state_.p, sizeof(KState), cudaMemcpyDeviceToHost, st));
+    PFG_CUDA(cudaStreamSynchronize(st));
+    h = *host_state_;
+}
+
+double Krylov::true_residual(const DevMatrix &A, const double *b, const double *x, double *r, cudaStream_t st)
+{
+    const int g = row_grid(A.nb);
+    if (A.bs == 3)
+        k_residual64<3><<<g, kThreads, 0, st>>>(A.view<double>(), b, x, r, state_.p, partials_.p, ticket_.p);
+    else
+        k_residual64<1><<<g, kThreads, 0, st>>>(A.view<double>(), b, x, r, state_.p, partials_.p, ticket_.p);
+    PFG_CUDA(cudaGetLastError());
+    ++launches_;
+    KState h;
+    read_state(h, st);
+    const double bn = sqrt(h.bb);
+    return bn > 0 ? sqrt(h.true_rr) / bn : sqrt(h.true_rr);
+}
+
+// Capture `body` (a sequence of kernel launches on `st`) into an executable graph.
+template <typename F>
+static cudaGraphExec_t capture(cudaStream_t st, F &&body)
+{
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    PFG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        body();
+    } catch (...) {
+        cudaStreamEndCapture(st, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    PFG_CUDA(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    PFG_CUDA(e);
+    return ge;
+}
+
+static uint64_t mix_key(std::initializer_list<uint64_t> v)
+{
+    uint64_t h = 1469598103934665603ull;
+    for (uint64_t x : v) {
+        h ^= x + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
+    }
+    return h;
+}
+
+template <int BS>
+static void cg_chunk(const BsrView<double> &A64, const BsrView<float> &A32, bool mixed, int chunk, int64_t nb,
+                     double *x, double *r, double *z, double *pA, double *pB, double *q, const double *dinv,
+                     float *x32, float *r32, float *z32, float *pA32, float *pB32, float *q32, const float *dinv32,
+                     int pc, KState *S, double *pd, float *pf, unsigned *tk, double tol, double delta, int itrmax,
+                     cudaStream_t st)
+{
+    const int g = Krylov::row_grid(nb);
+    for (int it = 0; it < chunk; ++it) {
+        if (!mixed) {
+            k_cg_spmv<BS, double><<<g, kThreads, 0, st>>>(A64, z, pA, pB, q, S, pd, pf, tk);
+            k_cg_update<BS, double><<<g, kThreads, 0, st>>>(nb, x, r, z, pA, pB, q, dinv, pc, S, pd, pf, tk, tol,
+                                                            delta, itrmax);
+        } else {
+            k_cg_spmv<BS, float><<<g, kThreads, 0, st>>>(A32, z32, pA32, pB32, q32, S, pd, pf, tk);
+            k_cg_update<BS, float><<<g, kThreads, 0, st>>>(nb, x32, r32, z32, pA32, pB32, q32, dinv32, pc, S, pd,
+                                                           pf, tk, tol, delta, itrmax);
+        }
+    }
+    PFG_CUDA(cudaGetLastError());
+}
+
+template <int BS>
+static void bicg_chunk(const BsrView<double> &A64, const BsrView<float> &A32, bool mixed, int chunk, int64_t nb,
+                       double *x, double *r, double *r0, double *pA, double *pB, double *yA, double *yB, double *e,
+                       double *v, float *x32, float *r32, float *r032, float *pA32, float *pB32, float *yA32,
+                       float *yB32, float *e32, float *v32, KState *S, double *pd, float *pf, unsigned *tk,
+                       int stop_rule, double er0, double tol, double delta, int itrmax, cudaStream_t st)
+{
+    const int g = Krylov::row_grid(nb);
+    for (int it = 0; it < chunk; ++it) {
+        if (!mixed) {
+            k_bicg_spmv1<BS, double><<<g, kThreads, 0, st>>>(A64, r, r0, pA, pB, yA, yB, S, pd, pf, tk);
+            k_bicg_spmv2<BS, double><<<g, kThreads, 0, st>>>(A64, r, yA, yB, e, v, S, pd, pf, tk);
+            k_bicg_update<BS, double><<<g, kThreads, 0, st>>>(nb, x, r, r0, pA, pB, e, v, S, pd, pf, tk, stop_rule,
+                                                              er0, tol, delta, itrmax);
+        } else {
+            k_bicg_spmv1<BS, float><<<g, kThreads, 0, st>>>(A32, r32, r032, pA32, pB32, yA32, yB32, S, pd, pf, tk);
+            k_bicg_spmv2<BS, float><<<g, kThreads, 0, st>>>(A32, r32, yA32, yB32, e32, v32, S, pd, pf, tk);
+            k_bicg_update<BS, float><<<g, kThreads, 0, st>>>(nb, x32, r32, r032, pA32, pB32, e32, v32, S, pd, pf,
+                                                             tk, PFG_STOP_TRUE_RELATIVE, er0, tol, delta, itrmax);
+        }
+    }
+    PFG_CUDA(cudaGetLastError());
+}
+
+SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfig &cfg_in, cudaStream_t st)
+{
+    KConfig cfg = cfg_in;
+    PFG_CHECK(A.nb > 0, PFG_E_STATE, "empty matrix");
+    PFG_CHECK(cfg.algorithm == PFG_ALG_CG || cfg.algorithm == PFG_ALG_BICGSTAB, PFG_E_ARG, "unknown algorithm");
+    PFG_CHECK(cfg.precision == PFG_PREC_FP64 || cfg.precision == PFG_PREC_MIXED, PFG_E_ARG, "unknown precision");
+    PFG_CHECK(cfg.precond >= PFG_PC_NONE && cfg.precond <= PFG_PC_BLOCK_JACOBI, PFG_E_ARG, "unknown precond");
+    PFG_CHECK(!(cfg.algorithm == PFG_ALG_BICGSTAB && cfg.precond != PFG_PC_NONE), PFG_E_UNSUPPORTED,
+              "BiCGSTAB runs unpreconditioned (as bicgstab_CRS_2); use CG for preconditioning");
+    if (cfg.itrmax <= 0) cfg.itrmax = 100000;
+    if (cfg.graph_chunk <= 0) cfg.graph_chunk = 32;
+    if (cfg.precision == PFG_PREC_MIXED) cfg.stop_rule = PFG_STOP_TRUE_RELATIVE;
+    if (cfg.reliable_delta <= 0.0 || cfg.reliable_delta >= 1.0) cfg.reliable_delta = 0.1;
+    prepare(A, cfg, st);
+    launches_ = 0;
+    cudaEvent_t e0, e1;
+    PFG_CUDA(cudaEventCreate(&e0));
+    PFG_CUDA(cudaEventCreate(&e1));
+    PFG_CUDA(cudaEventRecord(e0, st));
+    SolveResult res;
+    try {
+        if (cfg.precision == PFG_PREC_MIXED)
+            res = run_mixed(A, b, x, cfg, st);
+        else if (cfg.algorithm == PFG_ALG_CG)
+            res = run_cg64(A, b, x, cfg, st);
+        else
+            res = run_bicgstab64(A, b, x, cfg, st);
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    PFG_CUDA(cudaEventRecord(e1, st));
+    PFG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    res.ms = ms;
+    res.launches = launches_;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return res;
+}
+
+SolveResult Krylov::run_cg64(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st)
+{
+    SolveResult res;
+    build_precond(A, cfg.precond, false, st);
+    const int64_t n = A.ndof();
+    const int g = row_grid(A.nb);
+    const uint64_t key = mix_key({1, (uint64_t)A.bs, (uint64_t)(uintptr_t)A.v64.p, (uint64_t)(uintptr_t)x,
+                                  (uint64_t)(uintptr_t)r_.p, (uint64_t)cfg.precond, (uint64_t)cfg.graph_chunk,
+                                  (uint64_t)cfg.itrmax, (uint64_t)(cfg.relative_er * 1e18), (uint64_t)n});
+    if (!graph_ || graph_key_ != key) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        auto body = [&]() {
+            if (A.bs == 3)
+                cg_chunk<3>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, z_.p, pA_.p,
+                            pB_.p, q_.p, dinv_.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                            cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
+                            cfg.reliable_delta, cfg.itrmax, st);
+            else
+                cg_chunk<1>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, z_.p, pA_.p,
+                            pB_.p, q_.p, dinv_.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                            cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
+                            cfg.reliable_delta, cfg.itrmax, st);
+        };
+        graph_ = capture(st, body);
+        graph_key_ = key;
+        graph_kernels_ = 2 * cfg.graph_chunk;
+    }
+    for (int restart = 0; restart < 20; ++restart) {
+        // r = b - A x (true residual), restart the recurrences from it
+        double rel = true_residual(A, b, x, r_.p, st);
+        res.rel_residual = rel;
+        if (rel <= cfg.relative_er) break;
+        PFG_CUDA(cudaMemsetAsync(pA_.p, 0, n * sizeof(double), st));
+        PFG_CUDA(cudaMemsetAsync(pB_.p, 0, n * sizeof(double), st));
+        if (A.bs == 3)
+            k_cg_restart<3, double><<<g, kThreads, 0, st>>>(A.nb, r_.p, z_.p, dinv_.p, cfg.precond, state_.p,
+                                                            partials_.p, partials32_.p, ticket_.p, 0);
+        else
+            k_cg_restart<1, double><<<g, kThreads, 0, st>>>(A.nb, r_.p, z_.p, dinv_.p, cfg.precond, state_.p,
+                                                            partials_.p, partials32_.p, ticket_.p, 0);
+        PFG_CUDA(cudaGetLastError());
+        ++launches_;
+        KState h;
+        for (;;) {
+            PFG_CUDA(cudaGraphLaunch(graph_, st));
+            launches_ += graph_kernels_;
+            read_state(h, st);
+            if (cfg.debug != 0) fprintf(stderr, "[pfg] CG64 iter %d |r|/|b| %.3e\n", h.iter, sqrt(h.rr / h.bb));
+            if (h.done) break;
+        }
+        res.iterations = h.iter;
+        res.iter_residual = sqrt(h.rr / h.bb);
+        if (h.status != PFG_OK) {
+            res.status = h.status;
+            res.rel_residual = true_residual(A, b, x, r_.p, st);
+            return res;
+        }
+        // clear done, keep the iteration count for itrmax
+        int zero = 0;
+        PFG_CUDA(cudaMemcpyAsync(&state_.p->done, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    }
+    res.rel_residual = true_residual(A, b, x, r_.p, st);
+    if (res.rel_residual > cfg.relative_er && res.status == PFG_OK) res.status = PFG_W_NOT_CONVERGED;
+    return res;
+}
+
+SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st)
+{
+    SolveResult res;
+    const int64_t n = A.ndof();
+    const int g = row_grid(A.nb);
+    const uint64_t key = mix_key({2, (uint64_t)A.bs, (uint64_t)(uintptr_t)A.v64.p, (uint64_t)(uintptr_t)x,
+                                  (uint64_t)(uintptr_t)r_.p, (uint64_t)cfg.stop_rule, (uint64_t)cfg.graph_chunk,
+                                  (uint64_t)cfg.itrmax, (uint64_t)(cfg.relative_er * 1e18),
+                                  (uint64_t)(cfg.er0 * 1e18), (uint64_t)n});
+    if (!graph_ || graph_key_ != key) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        auto body = [&]() {
+            if (A.bs == 3)
+                bicg_chunk<3>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, r0_.p,
+                              pA_.p, pB_.p, yA_.p, yB_.p, e_.p, v_.p, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              nullptr, nullptr, nullptr, nullptr, state_.p, partials_.p, partials32_.p, ticket_.p,
+                              cfg.stop_rule, cfg.er0, cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
+            else
+                bicg_chunk<1>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, r0_.p,
+                              pA_.p, pB_.p, yA_.p, yB_.p, e_.p, v_.p, nullptr, nullptr, nullptr, nullptr, nullptr,
+                              nullptr, nullptr, nullptr, nullptr, state_.p, partials_.p, partials32_.p, ticket_.p,
+                              cfg.stop_rule, cfg.er0, cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
+        };
+        graph_ = capture(st, body);
+        graph_key_ = key;
+        graph_kernels_ = 3 * cfg.graph_chunk;
+    }
+    const int max_restarts = cfg.stop_rule == PFG_STOP_REFERENCE ? 1 : 20;
+    for (int restart = 0; restart < max_restarts; ++restart) {
+        double rel = true_residual(A, b, x, r_.p, st);
+        res.rel_residual = rel;
+        if (cfg.stop_rule == PFG_STOP_TRUE_RELATIVE && rel <= cfg.relative_er) break;
+        PFG_CUDA(cudaMemsetAsync(pA_.p, 0, n * sizeof(double), st));
+        PFG_CUDA(cudaMemsetAsync(pB_.p, 0, n * sizeof(double), st));
+        PFG_CUDA(cudaMemsetAsync(yA_.p, 0, n * sizeof(double), st));
+        PFG_CUDA(cudaMemsetAsync(yB_.p, 0, n * sizeof(double), st));
+        k_bicg_restart<double><<<g, kThreads, 0, st>>>(n, r_.p, r0_.p, state_.p, partials_.p, partials32_.p,
+                                                       ticket_.p, 1, 0);
+        PFG_CUDA(cudaGetLastError());
+        ++launches_;
+        KState h;
+        for (;;) {
+            PFG_CUDA(cudaGraphLaunch(graph_, st));
+            launches_ += graph_kernels_;
+            read_state(h, st);
+            if (cfg.debug != 0) fprintf(stderr, "[pfg] BiCGSTAB64 iter %d |r| %.3e\n", h.iter, sqrt(h.rr));
+            if (h.done) break;
+        }
+        res.iterations = h.iter;
+        res.iter_residual = cfg.stop_rule == PFG_STOP_REFERENCE ? sqrt(h.rr / (h.rr1 > 0 ? h.rr1 : 1.0))
+                                                                : sqrt(h.rr / h.bb);
+        if (h.status != PFG_OK) {
+            res.status = h.status;
+            break;
+        }
+        int zero = 0;
+        PFG_CUDA(cudaMemcpyAsync(&state_.p->done, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+    }
+    res.rel_residual = true_residual(A, b, x, r_.p, st);
+    if (cfg.stop_rule == PFG_STOP_TRUE_RELATIVE && res.rel_residual > cfg.relative_er && res.status == PFG_OK)
+        res.status = PFG_W_NOT_CONVERGED;
+    return res;
+}
+
+SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st)
+{
+    SolveResult res;
+    const bool cg = cfg.algorithm == PFG_ALG_CG;
+    if (!A.v32_valid) {
+        make_v32(A, st);
+        ++launches_;
+    }
+    build_precond(A, cfg.precond, true, st);
+    const int64_t n = A.ndof();
+    const int g = row_grid(A.nb);
+    const int gv = grid_for(n, 256, sm_count() * 8);
+    const uint64_t key = mix_key({3, (uint64_t)cg, (uint64_t)A.bs, (uint64_t)(uintptr_t)A.v32.p,
+                                  (uint64_t)(uintptr_t)x32_.p, (uint64_t)(uintptr_t)r32_.p, (uint64_t)cfg.precond,
+                                  (uint64_t)cfg.graph_chunk, (uint64_t)cfg.itrmax,
+                                  (uint64_t)(cfg.relative_er * 1e18), (uint64_t)(cfg.reliable_delta * 1e18),
+                                  (uint64_t)n});
+    if (!graph_ || graph_key_ != key) {
+        if (graph_) cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+        auto body = [&]() {
+            if (cg) {
+                if (A.bs == 3)
+                    cg_chunk<3>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                                nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p, z32_.p, pA32_.p, pB32_.p,
+                                q32_.p, dinv32_.p, cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p,
+                                cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
+                else
+                    cg_chunk<1>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                                nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p, z32_.p, pA32_.p, pB32_.p,
+                                q32_.p, dinv32_.p, cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p,
+                                cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
+            } else {
+                if (A.bs == 3)
+                    bicg_chunk<3>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p,
+                                  r032_.p, pA32_.p, pB32_.p, yA32_.p, yB32_.p, e32_.p, v32_.p, state_.p, partials_.p,
+                                  partials32_.p, ticket_.p, PFG_STOP_TRUE_RELATIVE, cfg.er0, cfg.relative_er,
+                                  cfg.reliable_delta, cfg.itrmax, st);
+                else
+                    bicg_chunk<1>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p,
+                                  r032_.p, pA32_.p, pB32_.p, yA32_.p, yB32_.p, e32_.p, v32_.p, state_.p, partials_.p,
+                                  partials32_.p, ticket_.p, PFG_STOP_TRUE_RELATIVE, cfg.er0, cfg.relative_er,
+                                  cfg.reliable_delta, cfg.itrmax, st);
+            }
+        };
+        graph_ = capture(st, body);
+        graph_key_ = key;
+        graph_kernels_ = (cg ? 2 : 3) * cfg.graph_chunk;
+    }
+    // initial FP64 residual and first replacement
+    PFG_CUDA(cudaMemsetAsync(x32_.p, 0, n * sizeof(float), st));
+    PFG_CUDA(cudaMemsetAsync(pA32_.p, 0, n * sizeof(float), st));
+    PFG_CUDA(cudaMemsetAsync(pB32_.p, 0, n * sizeof(float), st));
+    if (!cg) {
+        PFG_CUDA(cudaMemsetAsync(yA32_.p, 0, n * sizeof(float), st));
+        PFG_CUDA(cudaMemsetAsync(yB32_.p, 0, n * sizeof(float), st));
+    }
+    bool first = true;
+    KState h;
+    memset(&h, 0, sizeof(h));
+    for (;;) {
+        // residual replacement: x64 += x32; r64 = b - A64 x64; r32 = r64
+        if (!first) {
+            k_fold<<<gv, 256, 0, st>>>(n, x, x32_.p);
+            PFG_CUDA(cudaGetLastError());
+            ++launches_;
+        }
+        const double rel = true_residual(A, b, x, r_.p, st);
+        res.rel_residual = rel;
+        k_replace<<<gv, 256, 0, st>>>(n, r_.p, r32_.p, state_.p, cfg.relative_er);
+        PFG_CUDA(cudaGetLastError());
+        launches_ += 2;  // k_replace and the restart below
+        if (cg) {
+            if (A.bs == 3)
+                k_cg_restart<3, float><<<g, kThreads, 0, st>>>(A.nb, r32_.p, z32_.p, dinv32_.p, cfg.precond,
+                                                               state_.p, partials_.p, partials32_.p, ticket_.p,
+                                                               first ? 0 : 1);
+            else
+                k_cg_restart<1, float><<<g, kThreads, 0, st>>>(A.nb, r32_.p, z32_.p, dinv32_.p, cfg.precond,
+                                                               state_.p, partials_.p, partials32_.p, ticket_.p,
+                                                               first ? 0 : 1);
+        } else {
+            k_bicg_restart<float><<<g, kThreads, 0, st>>>(n, r32_.p, r032_.p, state_.p, partials_.p, partials32_.p,
+                                                          ticket_.p, first ? 1 : 0, first ? 0 : 1);
+        }
+        PFG_CUDA(cudaGetLastError());
+        first = false;
+        read_state(h, st);
+        if (cfg.debug != 0)
+            fprintf(stderr, "[pfg] mixed iter %d replacement %d |b-Ax|/|b| %.3e\n", h.iter, h.replacements, rel);
+        if (h.done) break;
+        for (;;) {
+            PFG_CUDA(cudaGraphLaunch(graph_, st));
+            launches_ += graph_kernels_;
+            read_state(h, st);
+            if (h.done || h.need_update) break;
+        }
+        if (h.done && h.status != PFG_OK) {
+            // fold what was computed, report the true residual
+            k_fold<<<gv, 256, 0, st>>>(n, x, x32_.p);
+            PFG_CUDA(cudaGetLastError());
+            ++launches_;
+            res.rel_residual = true_residual(A, b, x, r_.p, st);
+            break;
+        }
+    }
+    res.status = h.status;
+    res.iterations = h.iter;
+    res.replacements = h.replacements;
+    res.iter_residual = sqrt((double)h.rr32 / (h.bb > 0 ? h.bb : 1.0));
+    if (res.status == PFG_OK && res.rel_residual > cfg.relative_er) res.status = PFG_W_NOT_CONVERGED;
+    return res;
+}
+
+__global__ void k_fill(float *a, int64_t n, float v)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+__global__ void k_fill(double *a, int64_t n, double v)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
+void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
+{
+    PFG_CHECK(kernel >= 0 && kernel <= 2 && reps > 0, PFG_E_ARG, "bad profile request");
+    const int64_t n = A.ndof();
+    const double idx = (double)A.nnzb * 4.0 + (double)(A.nb + 1) * 8.0;  // block columns + row pointers
+    if (kernel != 0 && !A.v32_valid) make_v32(A, st);
+    const int gv = grid_for(n, 256, sm_count() * 8);
+    const int g = row_grid(A.nb);
+    DevBuf<double> x64, y64;
+    DevBuf<float> x32, y32, p32, q32;
+    KState hs;
+    memset(&hs, 0, sizeof(hs));
+    hs.rho32 = 1.0f;
+    hs.beta32 = 0.5f;
+    if (!state_.p) state_.alloc(1);
+    if (!ticket_.p) {
+        ticket_.alloc(1);
+        PFG_CUDA(cudaMemsetAsync(ticket_.p, 0, sizeof(unsigned), st));
+    }
+    partials_.ensure((size_t)g * 4 + 8);
+    partials32_.ensure((size_t)g * 8 + 16);
+    PFG_CUDA(cudaMemcpyAsync(state_.p, &hs, sizeof(KState), cudaMemcpyHostToDevice, st));
+    auto launch = [&]() {
+        if (kernel == 0) {
+            if (A.bs == 3) k_spmv<3, double><<<g, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
+            else k_spmv<1, double><<<g, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
+        } else if (kernel == 1) {
+            if (A.bs == 3) k_spmv<3, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, y32.p);
+            else k_spmv<1, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, y32.p);
+        } else {
+            if (A.bs == 3)
+                k_cg_spmv<3, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
+                                                            partials_.p, partials32_.p, ticket_.p);
+            else
+                k_cg_spmv<1, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
+                                                            partials_.p, partials32_.p, ticket_.p);
+        }
+    };
+    if (kernel == 0) {
+        x64.alloc((size_t)n);
+        y64.alloc((size_t)n);
+        k_fill<<<gv, 256, 0, st>>>(x64.p, n, 1.0);
+        bytes = (double)A.nnzb * 9.0 * 8.0 + idx + 2.0 * (double)n * 8.0;
+    } else {
+        x32.alloc((size_t)n);
+        y32.alloc((size_t)n);
+        k_fill<<<gv, 256, 0, st>>>(x32.p, n, 1.0f);
+        bytes = (double)A.nnzb * 9.0 * 4.0 + idx + 2.0 * (double)n * 4.0;
+        if (kernel == 2) {
+            p32.alloc((size_t)n);
+            q32.alloc((size_t)n);
+            k_fill<<<gv, 256, 0, st>>>(p32.p, n, 1.0f);
+            bytes += 2.0 * (double)n * 4.0;  // p_old read, p_new write on top of the SpMV
+        }
+    }
+    PFG_CUDA(cudaGetLastError());
+    for (int w = 0; w < 3; ++w) launch();  // warm-up
+    cudaEvent_t e0, e1;
+    PFG_CUDA(cudaEventCreate(&e0));
+    PFG_CUDA(cudaEventCreate(&e1));
+    PFG_CUDA(cudaEventRecord(e0, st));
+    for (int r = 0; r < reps; ++r) launch();
+    PFG_CUDA(cudaEventRecord(e1, st));
+    PFG_CUDA(cudaEventSynchronize(e1));
+    PFG_CUDA(cudaGetLastError());
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ms = (double)t / reps;
+    if (kernel == 2) {
+        KState h;
+        read_state(h, st);
+        PFG_CHECK(!h.done, PFG_E_BREAKDOWN, "profiled CG SpMV hit p.Ap <= 0 (matrix not positive definite)");
+    }
+}
+
+}  // namespace pfg

@@ -1,0 +1,113 @@
+// krylov.cuh -- device-resident CG / BiCGSTAB on the block-row layout.
+//
+// The host-level solver objects are declared here and implemented in
+// krylov.cu; the FEMSolver handle (femsolver.cu) owns one of each.
+#pragma once
+
+#include "bsr.cuh"
+
+namespace pfg {
+
+// Scalars of one solve, resident in device memory.  Kernels read what they
+// need at entry and the last CTA of each reduction writes the new values, so
+// no scalar ever travels to the host inside the iteration loop.
+struct KState {
+    // FP64 recurrences
+    double rho, rho_prev, alpha, beta, pq, rr, bb, rr1, c1, c2, c3, ev, vv;
+    // FP32 recurrences of the mixed-precision inner iteration
+    float rho32, alpha32, beta32, rr32, c1_32, c2_32, c3_32, rmax32;
+    double true_rr;        // |b - A x|^2 in FP64 at the last residual replacement
+    int iter;              // inner iterations done
+    int done;              // 1 = stop (converged, breakdown or itrmax)
+    int need_update;       // mixed: 1 = fold x32 into x64 and replace r
+    int parity;            // which of the ping-pong buffers holds the current p
+    int status;            // PFG_OK, PFG_E_BREAKDOWN, PFG_W_NOT_CONVERGED
+    int replacements;      // mixed: number of FP64 residual replacements
+    int pad[2];
+};
+
+struct KConfig {
+    int algorithm;     // PFG_ALG_*
+    int precision;     // PFG_PREC_*
+    int precond;       // PFG_PC_*
+    int stop_rule;     // PFG_STOP_*
+    int itrmax;
+    double er0, relative_er, reliable_delta;
+    int graph_chunk;
+    int debug;
+};
+
+struct SolveResult {
+    int status = PFG_OK;
+    int iterations = 0;
+    int replacements = 0;
+    int launches = 0;  // kernels launched by the solve, inside graphs included
+    double rel_residual = 0.0;
+    double iter_residual = 0.0;
+    double ms = 0.0;
+};
+
+// Matrix owned on the device in the block-row layout.  v32 is the FP32 copy
+// used by the mixed-precision inner iterations (built on demand).
+struct DevMatrix {
+    int bs = 3;
+    int64_t nb = 0, nnzb = 0;
+    DevBuf<int64_t> rp;
+    DevBuf<int> col;
+    DevBuf<double> v64;
+    DevBuf<float> v32;
+    bool v32_valid = false;
+    int64_t ndof() const { return nb * bs; }
+    template <typename T>
+    BsrView<T> view() const;
+};
+template <>
+inline BsrView<double> DevMatrix::view<double>() const { return BsrView<double>{nb, nnzb, rp.p, col.p, v64.p}; }
+template <>
+inline BsrView<float> DevMatrix::view<float>() const { return BsrView<float>{nb, nnzb, rp.p, col.p, v32.p}; }
+
+class Krylov {
+  public:
+    Krylov();
+    ~Krylov();
+    // Solve A x = b (device vectors of length A.ndof()); x holds x0 on entry.
+    SolveResult solve(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
+    // y = A x in FP64 / FP32 (plain SpMV, used by the C ABI and the tests).
+    static void spmv64(const DevMatrix &A, const double *x, double *y, cudaStream_t st);
+    static void spmv32(const DevMatrix &A, const float *x, float *y, cudaStream_t st);
+    static void make_v32(DevMatrix &A, cudaStream_t st);
+    // Grid size used for the row loops (a multiple of the SM count).
+    static int row_grid(int64_t nb);
+    // Mean ms per launch of one kernel over `reps` launches (CUDA events on st)
+    // and the algorithmic bytes of one launch.  kernel: 0 FP64 SpMV, 1 FP32
+    // SpMV, 2 FP32 CG SpMV with fused direction update.
+    void profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes);
+
+  private:
+    void prepare(const DevMatrix &A, const KConfig &cfg, cudaStream_t st);
+    void build_precond(const DevMatrix &A, int precond, bool fp32, cudaStream_t st);
+    SolveResult run_cg64(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
+    SolveResult run_bicgstab64(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
+    SolveResult run_mixed(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
+    void read_state(KState &h, cudaStream_t st);
+    double true_residual(const DevMatrix &A, const double *b, const double *x, double *r, cudaStream_t st);
+
+    int64_t n_ = 0;
+    int bs_ = 3;
+    // FP64 work vectors
+    DevBuf<double> r_, r0_, z_, pA_, pB_, q_, yA_, yB_, e_, v_, dinv_;
+    // FP32 work vectors
+    DevBuf<float> r32_, r032_, z32_, pA32_, pB32_, q32_, yA32_, yB32_, e32_, v32_, x32_, dinv32_;
+    DevBuf<double> partials_;
+    DevBuf<float> partials32_;
+    DevBuf<unsigned int> ticket_;
+    DevBuf<KState> state_;
+    KState *host_state_ = nullptr;  // pinned mirror
+    // cached CUDA graphs of one chunk of iterations
+    cudaGraphExec_t graph_ = nullptr;
+    uint64_t graph_key_ = 0;
+    int graph_kernels_ = 0;  // kernels captured in graph_
+    int launches_ = 0;       // launch count of the current solve
+};
+
+}  // namespace pfg

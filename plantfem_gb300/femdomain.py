@@ -1,0 +1,108 @@
+"""FEMDomain: the structured hex8 mesh side of plantFEM's FEMDomain_.
+
+Host-side mesh generation and selection (O(nodes) work, numpy).  Mirrors
+``FEMDomain_%create("Cube3D", ...)`` (FEMDomainClass.f90:7215-7310 ->
+MeshClass.f90:6348-6361, rectangular2D :6745-6805, Convert2Dto3D
+:6992-7087), ``resize`` (FEMDomainClass.f90:2123-2130 -> MeshClass.f90:892-937)
+and ``select`` (FEMDomainClass.f90:12854-12910).  Arrays keep the reference's
+layout: ``nodcoord`` (nn, 3) float64 and ``elemnod`` (ne, 8) int32 with 1-based
+node ids.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+class FEMDomain:
+    def __init__(self):
+        self.nodcoord = np.zeros((0, 3))
+        self.elemnod = np.zeros((0, 8), dtype=np.int32)
+
+    # ------------------------------------------------------------------ create
+    def create(self, meshtype: str = "Cube3D", x_num: int = 10, y_num: int = 10, z_num: int = 10,
+               x_len: float = 1.0, y_len: float = 1.0, z_len: float = 1.0) -> "FEMDomain":
+        if meshtype not in ("Cube", "Cube3D", "cube3D"):
+            raise NotImplementedError(f"meshtype {meshtype!r}: only Cube3D is on this path")
+        nx, ny, nz = int(x_num), int(y_num), int(z_num)
+        if min(nx, ny, nz) < 1:
+            raise ValueError("x_num, y_num, z_num must be >= 1")
+        i = np.arange(nx + 1, dtype=np.float64)
+        j = np.arange(ny + 1, dtype=np.float64)
+        k = np.arange(nz + 1, dtype=np.float64)
+        # coordinate = len / num * (index - 1)  (MeshClass.f90:6765-6766, :7041)
+        xs = x_len / float(nx) * i
+        ys = y_len / float(ny) * j
+        zs = z_len / float(nz) * k
+        Z, Y, X = np.meshgrid(zs, ys, xs, indexing="ij")
+        self.nodcoord = np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1)
+        # quads (MeshClass.f90:6794-6803), then layers (:7062-7068)
+        ii, jj = np.meshgrid(np.arange(1, nx + 1), np.arange(ny), indexing="xy")
+        ii, jj = ii.ravel(), jj.ravel()
+        q = np.stack([ii + jj * (nx + 1), ii + 1 + jj * (nx + 1), nx + 2 + ii + jj * (nx + 1),
+                      nx + 1 + ii + jj * (nx + 1)], axis=1)
+        nn2 = (nx + 1) * (ny + 1)
+        layers = np.arange(nz)[:, None, None] * nn2
+        bottom = (q[None, :, :] + layers).reshape(-1, 4)
+        top = (q[None, :, :] + layers + nn2).reshape(-1, 4)
+        self.elemnod = np.ascontiguousarray(np.concatenate([bottom, top], axis=1), dtype=np.int32)
+        self.shape = (nx, ny, nz)
+        return self
+
+    def resize(self, x=None, y=None, z=None) -> "FEMDomain":
+        """Scale each axis to the given length (MeshClass.f90:917-936)."""
+        for d, L in enumerate((x, y, z)):
+            if L is None:
+                continue
+            span = self.nodcoord[:, d].max() - self.nodcoord[:, d].min()
+            self.nodcoord[:, d] = (L / span) * self.nodcoord[:, d]
+        return self
+
+    def deform(self, disp) -> "FEMDomain":
+        """nodcoord += reshape(disp, nn, nd) with plantFEM's row-major reshape
+        (FEMDomainClass.f90:14482, ArrayClass.f90:5328-5344)."""
+        self.nodcoord = self.nodcoord + np.asarray(disp, dtype=np.float64).reshape(self.nn(), 3)
+        return self
+
+    # ---------------------------------------------------------------- queries
+    def nn(self) -> int:
+        return int(self.nodcoord.shape[0])
+
+    def ne(self) -> int:
+        return int(self.elemnod.shape[0])
+
+    def nne(self) -> int:
+        return int(self.elemnod.shape[1])
+
+    def nd(self) -> int:
+        return 3
+
+    def x_min(self):
+        return float(self.nodcoord[:, 0].min())
+
+    def x_max(self):
+        return float(self.nodcoord[:, 0].max())
+
+    def y_min(self):
+        return float(self.nodcoord[:, 1].min())
+
+    def y_max(self):
+        return float(self.nodcoord[:, 1].max())
+
+    def z_min(self):
+        return float(self.nodcoord[:, 2].min())
+
+    def z_max(self):
+        return float(self.nodcoord[:, 2].max())
+
+    def select(self, x_min=None, x_max=None, y_min=None, y_max=None, z_min=None, z_max=None) -> np.ndarray:
+        """1-based ids of the nodes inside the box (FEMDomainClass.f90:12854-12910)."""
+        m = np.ones(self.nn(), dtype=bool)
+        for d, lo, hi in ((0, x_min, x_max), (1, y_min, y_max), (2, z_min, z_max)):
+            if lo is not None:
+                m &= self.nodcoord[:, d] >= lo
+            if hi is not None:
+                m &= self.nodcoord[:, d] <= hi
+        return (np.nonzero(m)[0] + 1).astype(np.int32)
+
+    def element_coords(self, element_id: int) -> np.ndarray:
+        return self.nodcoord[self.elemnod[element_id - 1] - 1]

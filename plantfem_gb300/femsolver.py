@@ -1,0 +1,268 @@
+"""FEMSolver: plantFEM's ``FEMSolver_`` call surface over the GPU library.
+
+Every method maps to one C-ABI entry point of ``include/pfg.h`` (see there
+for the reference line each replaces).  Public fields keep the reference's
+names and defaults (FEMSolverClass.f90:69-76).  Ids are 1-based as in the
+reference; arrays are numpy float64 / int32 / int64.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .femdomain import FEMDomain
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def _torch_sync():
+    import torch
+    torch.cuda.current_stream().synchronize()
+
+
+class FEMSolver:
+    # FEMSolver_ public configuration (FEMSolverClass.f90:69-76)
+    itrmax: int = 100000
+    er0: float = 1.0e-10
+    relative_er: float = 1.0e-10
+    debug: bool = False
+    use_LOBPCG: bool = False
+    LOBPCG_MAX_ITR: int = 100000
+    LOBPCG_TOL: float = 1.0e-6
+    LOBPCG_NUM_MODE: int = 5
+
+    def __init__(self, NumDomain: int = 1):
+        self._lib = N.load()
+        self._h = C.c_void_p()
+        self.init(NumDomain)
+
+    # ------------------------------------------------------------- lifecycle
+    def init(self, NumDomain: int = 1):
+        """FEMSolver_%init (FEMSolverClass.f90:174-327); one domain on this path."""
+        if NumDomain != 1:
+            raise NotImplementedError("multi-domain (overset) solves are outside this path")
+        if self._h:
+            self.remove()
+        N.check(self._lib.pfg_create(C.byref(self._h)))
+        self.domain = None
+        self.last_info = None
+
+    def remove(self):
+        """FEMSolver_%remove (FEMSolverClass.f90:1827-1889)."""
+        if getattr(self, "_h", None):
+            self._lib.pfg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.remove()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ------------------------------------------------------------- problem
+    def setDomain(self, FEMDomain: FEMDomain, DomainID: int = 1):
+        """FEMSolver_%setDomain (FEMSolverClass.f90:329-419)."""
+        if DomainID != 1:
+            raise NotImplementedError("DomainID must be 1")
+        dom = FEMDomain
+        xyz = _f64(np.asfortranarray(dom.nodcoord).T.reshape(-1))  # NodCoord(nn,3) column-major
+        en = _i32(np.asfortranarray(dom.elemnod).T.reshape(-1))    # ElemNod(ne,8) column-major
+        N.check(self._lib.pfg_set_mesh(self._h, dom.nn(), N.ptr(xyz), dom.ne(), 8, N.ptr(en)))
+        self.domain = dom
+
+    def setCRS(self, DOF=3, CRS=None):
+        """FEMSolver_%setCRS(DOF) (FEMSolverClass.f90:439) or setCRS(CRS_) (:421)."""
+        if CRS is not None:
+            row_ptr, col_idx, val = CRS
+            rp, ci, v = _i64(row_ptr), _i32(col_idx), _f64(val)
+            N.check(self._lib.pfg_set_crs_arrays(self._h, rp.shape[0] - 1, N.ptr(rp), N.ptr(ci), N.ptr(v)))
+            return
+        if not isinstance(DOF, (int, np.integer)):
+            return self.setCRS(CRS=DOF)
+        N.check(self._lib.pfg_set_crs(self._h, int(DOF)))
+
+    def getCRS(self):
+        """(row_ptr int64 1-based, col_idx int32 1-based, val) of the working matrix."""
+        n = C.c_int64()
+        nnz = C.c_int64()
+        N.check(self._lib.pfg_get_crs_size(self._h, C.byref(n), C.byref(nnz)))
+        rp = np.zeros(n.value + 1, dtype=np.int64)
+        ci = np.zeros(nnz.value, dtype=np.int32)
+        v = np.zeros(nnz.value)
+        N.check(self._lib.pfg_get_crs(self._h, N.ptr(rp), N.ptr(ci), N.ptr(v)))
+        return rp, ci, v
+
+    @property
+    def CRS_Index_Row(self):
+        return self.getCRS()[0]
+
+    @property
+    def CRS_Index_Col(self):
+        return self.getCRS()[1]
+
+    @property
+    def CRS_val(self):
+        return self.getCRS()[2]
+
+    def ndof(self) -> int:
+        n = C.c_int64()
+        N.check(self._lib.pfg_get_crs_size(self._h, C.byref(n), None))
+        return n.value
+
+    def setRHS(self, RHS):
+        """FEMSolver_%setRHS (FEMSolverClass.f90:431-437)."""
+        r = _f64(RHS)
+        N.check(self._lib.pfg_set_rhs(self._h, r.shape[0], N.ptr(r)))
+
+    @property
+    def CRS_RHS(self):
+        n = self.ndof()
+        r = np.zeros(n)
+        N.check(self._lib.pfg_get_rhs(self._h, n, N.ptr(r)))
+        return r
+
+    def setMatrix(self, DomainID: int, ElementID: int, DOF: int, Matrix):
+        """FEMSolver_%setMatrix (FEMSolverClass.f90:901-911)."""
+        m = _f64(np.asarray(Matrix, dtype=np.float64).T.reshape(-1))  # column-major 24x24
+        N.check(self._lib.pfg_set_matrix(self._h, DomainID, ElementID, DOF, N.ptr(m)))
+
+    def setMatrices(self, ElementIDs, Matrices):
+        ids = _i32(ElementIDs)
+        mats = _f64(np.asarray(Matrices, dtype=np.float64).transpose(0, 2, 1).reshape(-1))
+        N.check(self._lib.pfg_set_matrices(self._h, ids.shape[0], N.ptr(ids), N.ptr(mats)))
+
+    def setVector(self, DomainID: int, ElementID: int, DOF: int, Vector):
+        """FEMSolver_%setVector (FEMSolverClass.f90:913-920)."""
+        v = _f64(Vector)
+        N.check(self._lib.pfg_set_vector(self._h, DomainID, ElementID, DOF, N.ptr(v)))
+
+    def assembleStiffness(self, YoungModulus, PoissonRatio):
+        """Whole-mesh StiffnessMatrix(ElementID, E, v) + setMatrix loop, on the GPU."""
+        E = _f64(np.atleast_1d(YoungModulus))
+        nu = _f64(np.broadcast_to(np.atleast_1d(PoissonRatio), E.shape))
+        N.check(self._lib.pfg_assemble_stiffness(self._h, E.shape[0], N.ptr(E), N.ptr(nu)))
+
+    def assembleMass(self, Density, Lumped: bool = False):
+        rho = _f64(np.atleast_1d(Density))
+        N.check(self._lib.pfg_assemble_mass(self._h, rho.shape[0], N.ptr(rho), int(bool(Lumped))))
+
+    def assembleBodyForce(self, Density, Accel):
+        rho = _f64(np.atleast_1d(Density))
+        a = _f64(Accel)
+        N.check(self._lib.pfg_assemble_body_force(self._h, rho.shape[0], N.ptr(rho), N.ptr(a)))
+
+    def zeros(self):
+        """FEMSolver_%zeros (FEMSolverClass.f90:1310-1322)."""
+        N.check(self._lib.pfg_zeros(self._h))
+
+    def fix(self, DomainID: int = 1, IDs=None, FixValue: float | None = None, FixValues=None):
+        """FEMSolver_%fix (FEMSolverClass.f90:1073-1136)."""
+        ids = _i32(IDs)
+        vals = None if FixValues is None else _f64(FixValues)
+        N.check(self._lib.pfg_fix(self._h, ids.shape[0], N.ptr(ids), N.ptr(vals),
+                                  0.0 if FixValue is None else float(FixValue)))
+
+    # ------------------------------------------------------------- solving
+    def _opts(self, algorithm, precision, preconditioning, stop_rule):
+        alg = {"BiCGSTAB": N.ALG_BICGSTAB, "CG": N.ALG_CG}[algorithm or "BiCGSTAB"]
+        prec = {"fp64": N.PREC_FP64, "FP64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
+        pc = {None: N.PC_NONE, "None": N.PC_NONE, "PointJacobi": N.PC_JACOBI, "Jacobi": N.PC_JACOBI,
+              "BlockJacobi": N.PC_BLOCK_JACOBI}[preconditioning]
+        if stop_rule is None:
+            stop_rule = "reference" if prec == N.PREC_FP64 else "true_relative"
+        sr = {"reference": N.STOP_REFERENCE, "true_relative": N.STOP_TRUE_RELATIVE}[stop_rule]
+        return N.default_opts(algorithm=alg, precision=prec, precond=pc, stop_rule=sr, itrmax=int(self.itrmax),
+                              er0=float(self.er0), relative_er=float(self.relative_er), debug=int(bool(self.debug)))
+
+    def solve(self, algorithm: str | None = None, preconditioning: str | None = None, x0=None,
+              precision: str = "fp64", stop_rule: str | None = None) -> np.ndarray:
+        """x = FEMSolver_%solve([algorithm], [preconditioning], [x0]) (FEMSolverClass.f90:1697-1825).
+
+        Defaults reproduce the reference: unpreconditioned BiCGSTAB in FP64 with
+        its stop rule.  ``algorithm="CG"``, ``preconditioning="BlockJacobi"`` and
+        ``precision="mixed"`` select the GB300 forms.  Breakdown raises
+        (the reference stops); itrmax is reported in ``last_info``.
+        """
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule)
+        n = self.ndof()
+        x = np.zeros(n)
+        xi = None if x0 is None else _f64(x0)
+        info = N.Info()
+        N.check(self._lib.pfg_solve(self._h, C.byref(opts), N.ptr(xi), N.ptr(x), C.byref(info)))
+        self.last_info = info.as_dict()
+        return x
+
+    def solve_device(self, b, x, algorithm="CG", preconditioning="BlockJacobi", precision="mixed",
+                     stop_rule=None, stream=None):
+        """Solve with the already-eliminated matrix on device tensors b -> x
+        (x holds x0).  ``b`` and ``x`` are float64 CUDA tensors."""
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule)
+        info = N.Info()
+        if stream is None:
+            _torch_sync()  # the library works on its own stream: order after the caller's writes
+        N.check(self._lib.pfg_dev_solve(self._h, C.byref(opts), b.data_ptr(), x.data_ptr(), C.byref(info),
+                                        None if stream is None else C.c_void_p(stream)))
+        self.last_info = info.as_dict()
+        return info.as_dict()
+
+    def matvec_device(self, x, y, stream=None):
+        """y = K x on device float64 tensors."""
+        if stream is None:
+            _torch_sync()
+        N.check(self._lib.pfg_dev_spmv(self._h, x.data_ptr(), y.data_ptr(),
+                                       None if stream is None else C.c_void_p(stream)))
+        return y
+
+
+def crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector):
+    """GPU crs_spmv_real64 with the reference signature (SparseClass-c.c:131-143):
+    new_vector += A old_vector, 1-based CRS."""
+    lib = N.load()
+    v, rp, ci, x = _f64(val), _i64(row_ptr), _i32(col_idx), _f64(old_vector)
+    assert new_vector.dtype == np.float64 and new_vector.flags["C_CONTIGUOUS"]
+    N.check(lib.pfg_crs_spmv_real64(N.ptr(v), N.ptr(rp), N.ptr(ci), N.ptr(x), N.ptr(new_vector),
+                                    new_vector.shape[0], ci.shape[0]))
+    return new_vector
+
+
+def crs_spmv_real32(val, row_ptr, col_idx, old_vector, new_vector):
+    lib = N.load()
+    v = np.ascontiguousarray(val, dtype=np.float32)
+    rp, ci = _i64(row_ptr), _i32(col_idx)
+    x = np.ascontiguousarray(old_vector, dtype=np.float32)
+    assert new_vector.dtype == np.float32 and new_vector.flags["C_CONTIGUOUS"]
+    N.check(lib.pfg_crs_spmv_real32(N.ptr(v), N.ptr(rp), N.ptr(ci), N.ptr(x), N.ptr(new_vector),
+                                    new_vector.shape[0], ci.shape[0]))
+    return new_vector
+
+
+def linear_solver_crs(row_ptr, col_idx, val, rhs, x, algorithm="CG", precision="mixed",
+                      preconditioning="BlockJacobi", relative_er=1e-10, itrmax=100000, stop_rule=None):
+    """The LinearSolver(row_ptr, col_idx, val, rhs, x) plug-in of FEMSolver_%solve
+    (FEMSolverClass.f90:1632-1662) on the GPU; x is updated in place."""
+    lib = N.load()
+    s = FEMSolver.__new__(FEMSolver)
+    s.itrmax, s.er0, s.relative_er, s.debug = itrmax, 1e-10, relative_er, False
+    opts = FEMSolver._opts(s, algorithm, precision, preconditioning, stop_rule)
+    rp, ci, v, b = _i64(row_ptr), _i32(col_idx), _f64(val), _f64(rhs)
+    assert x.dtype == np.float64 and x.flags["C_CONTIGUOUS"]
+    info = N.Info()
+    N.check(lib.pfg_linear_solver_crs(N.ptr(rp), N.ptr(ci), N.ptr(v), N.ptr(b), N.ptr(x), b.shape[0], v.shape[0],
+                                      C.byref(opts), C.byref(info)))
+    return info.as_dict()
