@@ -197,22 +197,40 @@ def run_ours(args, ws, rank, local):
     out_extra = {}
     # reference algorithm on the GPU: unpreconditioned BiCGSTAB, reference stop rule
     if not args.skip_bicgstab:
-        x.zero_()
-        ib = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64",
-                            stop_rule="reference")
-        out_extra["bicgstab_fp64_reference_rule"] = {"iterations": ib["iterations"], "ms": ib["solve_ms"],
-                                                     "rel_residual": ib["rel_residual"], "status": ib["status"]}
-        x.zero_()
-        im = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="mixed",
-                            stop_rule="true_relative")
-        x.zero_()
-        i64 = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64",
-                             stop_rule="true_relative")
-        out_extra["bicgstab_true_rel_1e-10"] = {
-            "mixed": {"ms": im["solve_ms"], "iterations": im["iterations"], "status": im["status"]},
-            "fp64": {"ms": i64["solve_ms"], "iterations": i64["iterations"], "status": i64["status"]},
-            "speedup_mixed_vs_fp64": i64["solve_ms"] / im["solve_ms"] if im["solve_ms"] > 0 else None}
+        try:
+            out_extra.update(bicgstab_lines(s, b, x))
+        except Exception as e:  # reported, not fatal: the headline is the CG solve
+            out_extra["bicgstab_error"] = str(e)
 
+    run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_mixed, ms_step, value, f64_infos,
+             ms_f64, clk, setup_s, t0, t_pat, t_asm, out_extra)
+
+
+def bicgstab_lines(s, b, x):
+    """The reference algorithm (unpreconditioned BiCGSTAB) on the GPU: FP64 with
+    the reference stop rule, then FP64 and mixed to the true 1e-10 residual."""
+    out_extra = {}
+    x.zero_()
+    ib = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64", stop_rule="reference")
+    out_extra["bicgstab_fp64_reference_rule"] = {"iterations": ib["iterations"], "ms": ib["solve_ms"],
+                                                 "rel_residual": ib["rel_residual"], "status": ib["status"]}
+    x.zero_()
+    im = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="mixed",
+                        stop_rule="true_relative")
+    x.zero_()
+    i64 = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64",
+                         stop_rule="true_relative")
+    out_extra["bicgstab_true_rel_1e-10"] = {
+        "mixed": {"ms": im["solve_ms"], "iterations": im["iterations"], "status": im["status"]},
+        "fp64": {"ms": i64["solve_ms"], "iterations": i64["iterations"], "status": i64["status"]},
+        "speedup_mixed_vs_fp64": i64["solve_ms"] / im["solve_ms"] if im["solve_ms"] > 0 else None}
+    return out_extra
+
+
+def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_mixed, ms_step, value, f64_infos,
+             ms_f64, clk, setup_s, t0, t_pat, t_asm, out_extra):
+    import torch
+    from plantfem_gb300 import _native, linear_solver_crs
     # kernel roofline: the dominant kernel of the mixed solve is the FP32 block
     # SpMV with the fused direction update (k_cg_spmv<3,float>)
     prof = {}

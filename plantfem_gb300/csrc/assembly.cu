@@ -183,8 +183,8 @@ void build_pattern(const DevMesh &m, DevMatrix &K, cudaStream_t st)
     PFG_CUDA(cudaGetLastError());
     K.v64.alloc((size_t)nnzb * 9);
     PFG_CUDA(cudaMemsetAsync(K.v64.p, 0, (size_t)nnzb * 9 * sizeof(double), st));
-    K.v32.release();
-    K.v32_valid = false;
+    // new pattern: every derived copy (FP32, sliced) is stale
+    K.pattern_changed();
     PFG_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -470,7 +470,7 @@ void assemble_elements(const DevMesh &m, DevMatrix &K, int kind, const double *p
                                                       K.v64.p, 0, nullptr, err.p);
         PFG_CUDA(cudaGetLastError());
     }
-    K.v32_valid = false;
+    K.values_changed();
     check_err(err, st);
 }
 
@@ -574,7 +574,7 @@ void scatter_element_matrices(const DevMesh &m, DevMatrix &K, int64_t count, con
     k_scatter_mats<<<grid_for(count * 64, 256, 152 * 16), 256, 0, st>>>(count, ids, mats, m.conn.p, m.ne, K.rp.p,
                                                                         K.col.p, K.v64.p, err.p);
     PFG_CUDA(cudaGetLastError());
-    K.v32_valid = false;
+    K.values_changed();
     int h = 0;
     PFG_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     PFG_CUDA(cudaStreamSynchronize(st));
@@ -768,7 +768,7 @@ void apply_dirichlet(DevMatrix &K, double *rhs, const uint8_t *fixed, const doub
     else
         k_dirichlet<1><<<g, 128, 0, st>>>(K.nb, K.rp.p, K.col.p, K.v64.p, rhs, fixed, fixval);
     PFG_CUDA(cudaGetLastError());
-    K.v32_valid = false;
+    K.values_changed();
 }
 
 __global__ void k_restore_fixed(int64_t n, double *x, const uint8_t *fixed, const double *fixval)
@@ -854,16 +854,16 @@ void import_crs(int64_t n, int64_t nnz, const int64_t *row_ptr, const int32_t *c
         PFG_CUDA(cudaMemcpyAsync(&hok, ok.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         PFG_CUDA(cudaStreamSynchronize(st));
     }
-    K.v32.release();
-    K.v32_valid = false;
+    // keep the FP32 buffer (and its address): it is rebuilt from v64 on demand
+    K.pattern_changed();
     if (hok) {
         const int64_t nb = n / 3;
         K.bs = 3;
         K.nb = nb;
         K.nnzb = nnz / 9;
-        K.rp.alloc((size_t)nb + 1);
-        K.col.alloc((size_t)std::max<int64_t>(K.nnzb, 1));
-        K.v64.alloc((size_t)std::max<int64_t>(nnz, 1));
+        K.rp.resize((size_t)nb + 1);
+        K.col.resize((size_t)std::max<int64_t>(K.nnzb, 1));
+        K.v64.resize((size_t)std::max<int64_t>(nnz, 1));
         k_import_b3<<<grid_for(nb, 128, 152 * 16), 128, 0, st>>>(nb, row_ptr, col_idx, val, K.rp.p, K.col.p,
                                                                  K.v64.p);
         PFG_CUDA(cudaGetLastError());
@@ -871,9 +871,9 @@ void import_crs(int64_t n, int64_t nnz, const int64_t *row_ptr, const int32_t *c
         K.bs = 1;
         K.nb = n;
         K.nnzb = nnz;
-        K.rp.alloc((size_t)n + 1);
-        K.col.alloc((size_t)std::max<int64_t>(nnz, 1));
-        K.v64.alloc((size_t)std::max<int64_t>(nnz, 1));
+        K.rp.resize((size_t)n + 1);
+        K.col.resize((size_t)std::max<int64_t>(nnz, 1));
+        K.v64.resize((size_t)std::max<int64_t>(nnz, 1));
         int zero = 0;
         PFG_CUDA(cudaMemcpyAsync(ok.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
         k_import_b1<<<grid_for(std::max(n + 1, nnz), 256, 152 * 16), 256, 0, st>>>(n, row_ptr, col_idx, nnz, K.rp.p,

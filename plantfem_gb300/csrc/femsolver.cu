@@ -436,7 +436,7 @@ int pfg_zeros(pfg_solver *h)
         const int64_t nv = h->K.nnzb * h->K.bs * h->K.bs;
         PFG_CUDA(cudaMemsetAsync(h->K.v64.p, 0, nv * sizeof(double), h->st));
         PFG_CUDA(cudaMemsetAsync(h->rhs.p, 0, h->ndof() * sizeof(double), h->st));
-        h->K.v32_valid = false;
+        h->K.values_changed();
         PFG_CUDA(cudaStreamSynchronize(h->st));
     });
 }
@@ -609,23 +609,10 @@ int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const 
         PFG_CUDA(cudaMemcpyAsync(ci.p, col_idx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
         PFG_CUDA(cudaMemcpyAsync(v.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, h->st));
         PFG_CUDA(cudaMemcpyAsync(b.p, rhs, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-        const bool same = h->have_crs && h->ndof() == n && h->K.nnzb * h->K.bs * h->K.bs == nnz;
-        if (same) {
-            // same structure as last time: re-import values into the existing buffers
-            DevMatrix tmp;
-            import_crs(n, nnz, rp.p, ci.p, v.p, tmp, h->st);
-            if (tmp.bs == h->K.bs) {
-                std::swap(h->K.rp, tmp.rp);
-                std::swap(h->K.col, tmp.col);
-                std::swap(h->K.v64, tmp.v64);
-                h->K.v32_valid = false;
-            } else {
-                h->K = std::move(tmp);
-            }
-        } else {
-            import_crs(n, nnz, rp.p, ci.p, v.p, h->K, h->st);
-            h->have_crs = true;
-        }
+        // same sizes as the previous call: the import reuses the device
+        // buffers (same addresses), so the cached solver graphs stay valid
+        import_crs(n, nnz, rp.p, ci.p, v.p, h->K, h->st);
+        h->have_crs = true;
         h->x.ensure((size_t)n);
         PFG_CUDA(cudaMemcpyAsync(h->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
         const KConfig cfg = to_config(opts);

@@ -20,6 +20,8 @@
 //     Vorst 1996, as used for mixed-precision CG by Clark et al. 2010).  The
 //     stop test is always on that FP64 residual.
 #include <cmath>
+#include <mutex>
+#include <unordered_map>
 
 #include "krylov.cuh"
 
@@ -48,6 +50,28 @@ int Krylov::row_grid(int64_t nb)
     int64_t want = (nb + kWarps - 1) / kWarps;
     int64_t cap = (int64_t)sm_count() * 6;
     return (int)std::max<int64_t>(1, std::min(want, cap));
+}
+
+// Grid of exactly the CTAs that are resident at once (occupancy query, cached
+// per kernel), capped by the work: one wave, every warp striding over units.
+template <typename K>
+static int resident_grid(K kern, int64_t warps_needed)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void *, int> cache;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find((const void *)kern);
+        if (it == cache.end()) {
+            PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0));
+            cache[(const void *)kern] = per_sm;
+        } else {
+            per_sm = it->second;
+        }
+    }
+    const int64_t want = (warps_needed + kWarps - 1) / kWarps;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(per_sm, 1) * sm_count()));
 }
 
 template <int BS, typename T>
@@ -108,31 +132,59 @@ __global__ void __launch_bounds__(kThreads) k_spmv(BsrView<T> A, const T *__rest
     }
 }
 
-// r = b - A x in FP64; totals: rr = r.r and bb = b.b; stores into KState
-// (true_rr, bb) or, when mode==1, into rr/rr1 as the initial recursive residual.
+// Slice loop of the sliced-ELL kernels: warp w takes slices w, w + nw, ...;
+// lane l owns block row 32 s + l.
+#define PFG_SLICE_LOOP(A)                                                          \
+    const int lane = threadIdx.x & 31;                                             \
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;      \
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;                     \
+    for (int64_t s = w0; s < (A).ns; s += nw)
+
+// y = A x on the sliced copy (plain SpMV, profiling and the FP32 entry point).
+template <int BS, typename T>
+__global__ void __launch_bounds__(kThreads) k_spmv_sell(SellView<T> A, const T *__restrict__ x, T *__restrict__ y)
+{
+    PFG_SLICE_LOOP(A)
+    {
+        T acc[BS];
+        auto src = [&](int c, T(&xv)[BS]) {
+#pragma unroll
+            for (int i = 0; i < BS; ++i) xv[i] = __ldg(x + (int64_t)BS * c + i);
+        };
+        sell_row_product<BS>(A, s, lane, src, acc);
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb)
+#pragma unroll
+            for (int i = 0; i < BS; ++i) y[BS * row + i] = acc[i];
+    }
+}
+
+// r = b - A x in FP64; totals: true_rr = r.r and bb = b.b into KState.
 template <int BS>
-__global__ void __launch_bounds__(kThreads) k_residual64(BsrView<double> A, const double *__restrict__ b,
+__global__ void __launch_bounds__(kThreads) k_residual64(SellView<double> A, const double *__restrict__ b,
                                                          const double *__restrict__ x, double *__restrict__ r,
                                                          KState *S, double *partials, unsigned *ticket)
 {
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     double acc[2] = {0.0, 0.0};
-    for (int64_t row = w0; row < A.nb; row += nw) {
+    PFG_SLICE_LOOP(A)
+    {
         double y[BS];
         auto src = [&](int c, double(&xv)[BS]) {
 #pragma unroll
             for (int i = 0; i < BS; ++i) xv[i] = __ldg(x + (int64_t)BS * c + i);
         };
-        bsr_row_product<BS>(A, row, lane, src, y);
-        if (lane < BS) {
-            const int64_t i = (int64_t)BS * row + lane;
-            const double bi = b[i];
-            const double ri = bi - pick<BS>(y, lane);
-            r[i] = ri;
-            acc[0] = fma(ri, ri, acc[0]);
-            acc[1] = fma(bi, bi, acc[1]);
+        sell_row_product<BS>(A, s, lane, src, y);
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb) {
+#pragma unroll
+            for (int k = 0; k < BS; ++k) {
+                const int64_t i = (int64_t)BS * row + k;
+                const double bi = b[i];
+                const double ri = bi - y[k];
+                r[i] = ri;
+                acc[0] = fma(ri, ri, acc[0]);
+                acc[1] = fma(bi, bi, acc[1]);
+            }
         }
     }
     double tot[2];
@@ -240,7 +292,7 @@ __device__ __forceinline__ float st_alpha<float>(const KState *S) { return S->al
 // fin: alpha = rho / pq.
 template <int BS, typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_cg_spmv(BsrView<T> A, const T *__restrict__ z, T *pA, T *pB, T *__restrict__ q, KState *S, double *pd,
+    k_cg_spmv(SellView<T> A, const T *__restrict__ z, T *pA, T *pB, T *__restrict__ q, KState *S, double *pd,
               float *pf, unsigned *ticket)
 {
     if (S->done | S->need_update) return;
@@ -248,11 +300,9 @@ __global__ void __launch_bounds__(kThreads)
     const int par = S->parity;
     const T *pold = par ? pB : pA;
     T *pnew = par ? pA : pB;
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     typename Acc<T>::type acc[1] = {Acc<T>::zero()};
-    for (int64_t row = w0; row < A.nb; row += nw) {
+    PFG_SLICE_LOOP(A)
+    {
         T y[BS];
         auto src = [&](int c, T(&xv)[BS]) {
 #pragma unroll
@@ -261,14 +311,17 @@ __global__ void __launch_bounds__(kThreads)
                 xv[i] = fma(beta, __ldg(pold + j), __ldg(z + j));
             }
         };
-        bsr_row_product<BS>(A, row, lane, src, y);
-        if (lane < BS) {
-            const int64_t i = (int64_t)BS * row + lane;
-            const T pn = fma(beta, pold[i], z[i]);
-            const T qi = pick<BS>(y, lane);
-            pnew[i] = pn;
-            q[i] = qi;
-            Acc<T>::add(acc[0], pn, qi);
+        sell_row_product<BS>(A, s, lane, src, y);
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb) {
+#pragma unroll
+            for (int k = 0; k < BS; ++k) {
+                const int64_t i = (int64_t)BS * row + k;
+                const T pn = fma(beta, pold[i], z[i]);
+                pnew[i] = pn;
+                q[i] = y[k];
+                Acc<T>::add(acc[0], pn, y[k]);
+            }
         }
     }
     T tot[1];
@@ -389,11 +442,25 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------ BiCGSTAB kernels
+// FP64: the reference stops ("Bicgstab devide by zero", FEMSolverClass.f90:2266,2295).
+// FP32 inner iteration of the mixed solver: restart from the FP64 residual
+// instead; the host gives up after repeated breakdowns without progress.
+__device__ __forceinline__ void bicg_breakdown(KState *S, bool f64)
+{
+    if (f64) {
+        S->status = PFG_E_BREAKDOWN;
+        S->done = 1;
+    } else {
+        S->need_update = 1;
+        S->breakdowns += 1;
+    }
+}
+
 // y_new = A p_new, p_new = r + beta (p_old - c3 y_old) on the fly; c2 = r0.y_new;
 // fin: alpha = c1 / c2  (FEMSolverClass.f90:2236-2248, 2296).
 template <int BS, typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_bicg_spmv1(BsrView<T> A, const T *__restrict__ r, const T *__restrict__ r0, T *pA, T *pB, T *yA, T *yB,
+    k_bicg_spmv1(SellView<T> A, const T *__restrict__ r, const T *__restrict__ r0, T *pA, T *pB, T *yA, T *yB,
                  KState *S, double *pd, float *pf, unsigned *ticket)
 {
     if (S->done | S->need_update) return;
@@ -405,11 +472,9 @@ __global__ void __launch_bounds__(kThreads)
     T *pnew = par ? pA : pB;
     const T *yold = par ? yB : yA;
     T *ynew = par ? yA : yB;
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     typename Acc<T>::type acc[1] = {Acc<T>::zero()};
-    for (int64_t row = w0; row < A.nb; row += nw) {
+    PFG_SLICE_LOOP(A)
+    {
         T y[BS];
         auto src = [&](int c, T(&xv)[BS]) {
 #pragma unroll
@@ -418,22 +483,24 @@ __global__ void __launch_bounds__(kThreads)
                 xv[i] = fma(beta, fma(-c3, __ldg(yold + j), __ldg(pold + j)), __ldg(r + j));
             }
         };
-        bsr_row_product<BS>(A, row, lane, src, y);
-        if (lane < BS) {
-            const int64_t i = (int64_t)BS * row + lane;
-            const T pn = fma(beta, fma(-c3, yold[i], pold[i]), r[i]);
-            const T yi = pick<BS>(y, lane);
-            pnew[i] = pn;
-            ynew[i] = yi;
-            Acc<T>::add(acc[0], r0[i], yi);
+        sell_row_product<BS>(A, s, lane, src, y);
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb) {
+#pragma unroll
+            for (int k = 0; k < BS; ++k) {
+                const int64_t i = (int64_t)BS * row + k;
+                const T pn = fma(beta, fma(-c3, yold[i], pold[i]), r[i]);
+                pnew[i] = pn;
+                ynew[i] = y[k];
+                Acc<T>::add(acc[0], r0[i], y[k]);
+            }
         }
     }
     T tot[1];
     if (grid_total<1>(acc, pd, pf, ticket, tot)) {
         const double c2 = (double)tot[0];
         if (c2 == 0.0 || !finite_d(c2)) {
-            S->status = PFG_E_BREAKDOWN;
-            S->done = 1;
+            bicg_breakdown(S, f64);
         } else if (f64) {
             S->c2 = c2;
             S->alpha = S->c1 / c2;
@@ -448,18 +515,16 @@ __global__ void __launch_bounds__(kThreads)
 // (FEMSolverClass.f90:2254-2267).
 template <int BS, typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_bicg_spmv2(BsrView<T> A, const T *__restrict__ r, const T *yA, const T *yB, T *__restrict__ e,
+    k_bicg_spmv2(SellView<T> A, const T *__restrict__ r, const T *yA, const T *yB, T *__restrict__ e,
                  T *__restrict__ v, KState *S, double *pd, float *pf, unsigned *ticket)
 {
     if (S->done | S->need_update) return;
     const bool f64 = sizeof(T) == 8;
     const T alpha = f64 ? (T)S->alpha : (T)S->alpha32;
     const T *ynew = S->parity ? yA : yB;
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
-    for (int64_t row = w0; row < A.nb; row += nw) {
+    PFG_SLICE_LOOP(A)
+    {
         T y[BS];
         auto src = [&](int c, T(&xv)[BS]) {
 #pragma unroll
@@ -468,23 +533,25 @@ __global__ void __launch_bounds__(kThreads)
                 xv[i] = fma(-alpha, __ldg(ynew + j), __ldg(r + j));
             }
         };
-        bsr_row_product<BS>(A, row, lane, src, y);
-        if (lane < BS) {
-            const int64_t i = (int64_t)BS * row + lane;
-            const T ei = fma(-alpha, ynew[i], r[i]);
-            const T vi = pick<BS>(y, lane);
-            e[i] = ei;
-            v[i] = vi;
-            Acc<T>::add(acc[0], ei, vi);
-            Acc<T>::add(acc[1], vi, vi);
+        sell_row_product<BS>(A, s, lane, src, y);
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb) {
+#pragma unroll
+            for (int k = 0; k < BS; ++k) {
+                const int64_t i = (int64_t)BS * row + k;
+                const T ei = fma(-alpha, ynew[i], r[i]);
+                e[i] = ei;
+                v[i] = y[k];
+                Acc<T>::add(acc[0], ei, y[k]);
+                Acc<T>::add(acc[1], y[k], y[k]);
+            }
         }
     }
     T tot[2];
     if (grid_total<2>(acc, pd, pf, ticket, tot)) {
         const double vv = (double)tot[1];
         if (vv == 0.0 || !finite_d(vv) || !finite_d((double)tot[0])) {
-            S->status = PFG_E_BREAKDOWN;
-            S->done = 1;
+            bicg_breakdown(S, f64);
         } else if (f64) {
             S->ev = (double)tot[0];
             S->vv = vv;
@@ -557,11 +624,11 @@ __global__ void __launch_bounds__(kThreads)
             } else {
                 const float c2c3 = S->c2_32 * S->c3_32;
                 if (c2c3 == 0.f) {
-                    S->status = PFG_E_BREAKDOWN;
-                    S->done = 1;
+                    bicg_breakdown(S, false);
                 } else {
                     S->beta32 = (float)c1n / c2c3;
                     S->c1_32 = (float)c1n;
+                    S->breakdowns = 0;
                 }
             }
         }
@@ -713,7 +780,9 @@ void Krylov::prepare(const DevMatrix &A, const KConfig &cfg, cudaStream_t st)
             v32_.ensure(nn);
         }
     }
-    const int g = row_grid(A.nb);
+    // one partial per CTA and reduced value: bound by the most CTAs that can be
+    // resident (2048 threads per SM / kThreads)
+    const int g = sm_count() * (2048 / kThreads);
     partials_.ensure((size_t)g * 4 + 8);
     partials32_.ensure((size_t)g * 8 + 16);
     if (!ticket_.p) {
@@ -749,11 +818,12 @@ void Krylov::read_state(KState &h, cudaStream_t st)
 
 double Krylov::true_residual(const DevMatrix &A, const double *b, const double *x, double *r, cudaStream_t st)
 {
-    const int g = row_grid(A.nb);
+    PFG_CHECK(A.s64_valid, PFG_E_INTERNAL, "sliced FP64 copy not built");
+    const int g = A.bs == 3 ? resident_grid(k_residual64<3>, A.ns) : resident_grid(k_residual64<1>, A.ns);
     if (A.bs == 3)
-        k_residual64<3><<<g, kThreads, 0, st>>>(A.view<double>(), b, x, r, state_.p, partials_.p, ticket_.p);
+        k_residual64<3><<<g, kThreads, 0, st>>>(A.sell<double>(), b, x, r, state_.p, partials_.p, ticket_.p);
     else
-        k_residual64<1><<<g, kThreads, 0, st>>>(A.view<double>(), b, x, r, state_.p, partials_.p, ticket_.p);
+        k_residual64<1><<<g, kThreads, 0, st>>>(A.sell<double>(), b, x, r, state_.p, partials_.p, ticket_.p);
     PFG_CUDA(cudaGetLastError());
     ++launches_;
     KState h;
@@ -792,47 +862,79 @@ static uint64_t mix_key(std::initializer_list<uint64_t> v)
     return h;
 }
 
+uint64_t Krylov::graph_key(int kind, const DevMatrix &A, const void *x, const KConfig &cfg) const
+{
+    auto u = [](const void *p) { return (uint64_t)(uintptr_t)p; };
+    auto d = [](double v) {
+        uint64_t b;
+        memcpy(&b, &v, sizeof b);
+        return b;
+    };
+    return mix_key({(uint64_t)kind, (uint64_t)A.bs, (uint64_t)A.nb, (uint64_t)A.nnzb, u(A.rp.p), u(A.col.p),
+                    u(A.v64.p), u(A.v32.p), u(x), u(r_.p), u(r0_.p), u(z_.p), u(pA_.p), u(pB_.p), u(q_.p),
+                    u(yA_.p), u(yB_.p), u(e_.p), u(v_.p), u(dinv_.p), u(r32_.p), u(r032_.p), u(z32_.p),
+                    u(pA32_.p), u(pB32_.p), u(q32_.p), u(yA32_.p), u(yB32_.p), u(e32_.p), u(v32_.p), u(x32_.p),
+                    u(dinv32_.p), u(partials_.p), u(partials32_.p), u(ticket_.p), u(state_.p),
+                    (uint64_t)cfg.precond, (uint64_t)cfg.stop_rule, (uint64_t)cfg.graph_chunk, (uint64_t)cfg.itrmax,
+                    d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta)});
+}
+
 template <int BS>
-static void cg_chunk(const BsrView<double> &A64, const BsrView<float> &A32, bool mixed, int chunk, int64_t nb,
+static void cg_chunk(const SellView<double> &A64, const SellView<float> &A32, bool mixed, int chunk, int64_t nb,
                      double *x, double *r, double *z, double *pA, double *pB, double *q, const double *dinv,
                      float *x32, float *r32, float *z32, float *pA32, float *pB32, float *q32, const float *dinv32,
                      int pc, KState *S, double *pd, float *pf, unsigned *tk, double tol, double delta, int itrmax,
                      cudaStream_t st)
 {
-    const int g = Krylov::row_grid(nb);
-    for (int it = 0; it < chunk; ++it) {
-        if (!mixed) {
-            k_cg_spmv<BS, double><<<g, kThreads, 0, st>>>(A64, z, pA, pB, q, S, pd, pf, tk);
-            k_cg_update<BS, double><<<g, kThreads, 0, st>>>(nb, x, r, z, pA, pB, q, dinv, pc, S, pd, pf, tk, tol,
-                                                            delta, itrmax);
-        } else {
-            k_cg_spmv<BS, float><<<g, kThreads, 0, st>>>(A32, z32, pA32, pB32, q32, S, pd, pf, tk);
-            k_cg_update<BS, float><<<g, kThreads, 0, st>>>(nb, x32, r32, z32, pA32, pB32, q32, dinv32, pc, S, pd,
-                                                           pf, tk, tol, delta, itrmax);
+    const int64_t ns = mixed ? A32.ns : A64.ns;
+    if (!mixed) {
+        const int gs = resident_grid(k_cg_spmv<BS, double>, ns);
+        const int gu = resident_grid(k_cg_update<BS, double>, (nb + 31) / 32);
+        for (int it = 0; it < chunk; ++it) {
+            k_cg_spmv<BS, double><<<gs, kThreads, 0, st>>>(A64, z, pA, pB, q, S, pd, pf, tk);
+            k_cg_update<BS, double><<<gu, kThreads, 0, st>>>(nb, x, r, z, pA, pB, q, dinv, pc, S, pd, pf, tk, tol,
+                                                             delta, itrmax);
+        }
+    } else {
+        const int gs = resident_grid(k_cg_spmv<BS, float>, ns);
+        const int gu = resident_grid(k_cg_update<BS, float>, (nb + 31) / 32);
+        for (int it = 0; it < chunk; ++it) {
+            k_cg_spmv<BS, float><<<gs, kThreads, 0, st>>>(A32, z32, pA32, pB32, q32, S, pd, pf, tk);
+            k_cg_update<BS, float><<<gu, kThreads, 0, st>>>(nb, x32, r32, z32, pA32, pB32, q32, dinv32, pc, S, pd,
+                                                            pf, tk, tol, delta, itrmax);
         }
     }
     PFG_CUDA(cudaGetLastError());
 }
 
 template <int BS>
-static void bicg_chunk(const BsrView<double> &A64, const BsrView<float> &A32, bool mixed, int chunk, int64_t nb,
+static void bicg_chunk(const SellView<double> &A64, const SellView<float> &A32, bool mixed, int chunk, int64_t nb,
                        double *x, double *r, double *r0, double *pA, double *pB, double *yA, double *yB, double *e,
                        double *v, float *x32, float *r32, float *r032, float *pA32, float *pB32, float *yA32,
                        float *yB32, float *e32, float *v32, KState *S, double *pd, float *pf, unsigned *tk,
                        int stop_rule, double er0, double tol, double delta, int itrmax, cudaStream_t st)
 {
-    const int g = Krylov::row_grid(nb);
-    for (int it = 0; it < chunk; ++it) {
-        if (!mixed) {
-            k_bicg_spmv1<BS, double><<<g, kThreads, 0, st>>>(A64, r, r0, pA, pB, yA, yB, S, pd, pf, tk);
-            k_bicg_spmv2<BS, double><<<g, kThreads, 0, st>>>(A64, r, yA, yB, e, v, S, pd, pf, tk);
-            k_bicg_update<BS, double><<<g, kThreads, 0, st>>>(nb, x, r, r0, pA, pB, e, v, S, pd, pf, tk, stop_rule,
-                                                              er0, tol, delta, itrmax);
-        } else {
-            k_bicg_spmv1<BS, float><<<g, kThreads, 0, st>>>(A32, r32, r032, pA32, pB32, yA32, yB32, S, pd, pf, tk);
-            k_bicg_spmv2<BS, float><<<g, kThreads, 0, st>>>(A32, r32, yA32, yB32, e32, v32, S, pd, pf, tk);
-            k_bicg_update<BS, float><<<g, kThreads, 0, st>>>(nb, x32, r32, r032, pA32, pB32, e32, v32, S, pd, pf,
-                                                             tk, PFG_STOP_TRUE_RELATIVE, er0, tol, delta, itrmax);
+    const int64_t ns = mixed ? A32.ns : A64.ns;
+    const int64_t nvec = (nb * BS + 31) / 32;
+    if (!mixed) {
+        const int g1 = resident_grid(k_bicg_spmv1<BS, double>, ns);
+        const int g2 = resident_grid(k_bicg_spmv2<BS, double>, ns);
+        const int g3 = resident_grid(k_bicg_update<BS, double>, nvec);
+        for (int it = 0; it < chunk; ++it) {
+            k_bicg_spmv1<BS, double><<<g1, kThreads, 0, st>>>(A64, r, r0, pA, pB, yA, yB, S, pd, pf, tk);
+            k_bicg_spmv2<BS, double><<<g2, kThreads, 0, st>>>(A64, r, yA, yB, e, v, S, pd, pf, tk);
+            k_bicg_update<BS, double><<<g3, kThreads, 0, st>>>(nb, x, r, r0, pA, pB, e, v, S, pd, pf, tk, stop_rule,
+                                                               er0, tol, delta, itrmax);
+        }
+    } else {
+        const int g1 = resident_grid(k_bicg_spmv1<BS, float>, ns);
+        const int g2 = resident_grid(k_bicg_spmv2<BS, float>, ns);
+        const int g3 = resident_grid(k_bicg_update<BS, float>, nvec);
+        for (int it = 0; it < chunk; ++it) {
+            k_bicg_spmv1<BS, float><<<g1, kThreads, 0, st>>>(A32, r32, r032, pA32, pB32, yA32, yB32, S, pd, pf, tk);
+            k_bicg_spmv2<BS, float><<<g2, kThreads, 0, st>>>(A32, r32, yA32, yB32, e32, v32, S, pd, pf, tk);
+            k_bicg_update<BS, float><<<g3, kThreads, 0, st>>>(nb, x32, r32, r032, pA32, pB32, e32, v32, S, pd, pf,
+                                                              tk, PFG_STOP_TRUE_RELATIVE, er0, tol, delta, itrmax);
         }
     }
     PFG_CUDA(cudaGetLastError());
@@ -853,6 +955,9 @@ SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfi
     if (cfg.reliable_delta <= 0.0 || cfg.reliable_delta >= 1.0) cfg.reliable_delta = 0.1;
     prepare(A, cfg, st);
     launches_ = 0;
+    // the Krylov kernels read the sliced copy: FP64 always (residuals), FP32
+    // for the mixed inner iterations
+    build_sell(A, true, cfg.precision == PFG_PREC_MIXED, st);
     cudaEvent_t e0, e1;
     PFG_CUDA(cudaEventCreate(&e0));
     PFG_CUDA(cudaEventCreate(&e1));
@@ -887,20 +992,18 @@ SolveResult Krylov::run_cg64(DevMatrix &A, const double *b, double *x, const KCo
     build_precond(A, cfg.precond, false, st);
     const int64_t n = A.ndof();
     const int g = row_grid(A.nb);
-    const uint64_t key = mix_key({1, (uint64_t)A.bs, (uint64_t)(uintptr_t)A.v64.p, (uint64_t)(uintptr_t)x,
-                                  (uint64_t)(uintptr_t)r_.p, (uint64_t)cfg.precond, (uint64_t)cfg.graph_chunk,
-                                  (uint64_t)cfg.itrmax, (uint64_t)(cfg.relative_er * 1e18), (uint64_t)n});
+    const uint64_t key = graph_key(1, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
         if (graph_) cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
         auto body = [&]() {
             if (A.bs == 3)
-                cg_chunk<3>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, z_.p, pA_.p,
+                cg_chunk<3>(A.sell<double>(), SellView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, z_.p, pA_.p,
                             pB_.p, q_.p, dinv_.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                             cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
                             cfg.reliable_delta, cfg.itrmax, st);
             else
-                cg_chunk<1>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, z_.p, pA_.p,
+                cg_chunk<1>(A.sell<double>(), SellView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, z_.p, pA_.p,
                             pB_.p, q_.p, dinv_.p, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
                             cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
                             cfg.reliable_delta, cfg.itrmax, st);
@@ -953,21 +1056,18 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
     SolveResult res;
     const int64_t n = A.ndof();
     const int g = row_grid(A.nb);
-    const uint64_t key = mix_key({2, (uint64_t)A.bs, (uint64_t)(uintptr_t)A.v64.p, (uint64_t)(uintptr_t)x,
-                                  (uint64_t)(uintptr_t)r_.p, (uint64_t)cfg.stop_rule, (uint64_t)cfg.graph_chunk,
-                                  (uint64_t)cfg.itrmax, (uint64_t)(cfg.relative_er * 1e18),
-                                  (uint64_t)(cfg.er0 * 1e18), (uint64_t)n});
+    const uint64_t key = graph_key(2, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
         if (graph_) cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
         auto body = [&]() {
             if (A.bs == 3)
-                bicg_chunk<3>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, r0_.p,
+                bicg_chunk<3>(A.sell<double>(), SellView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, r0_.p,
                               pA_.p, pB_.p, yA_.p, yB_.p, e_.p, v_.p, nullptr, nullptr, nullptr, nullptr, nullptr,
                               nullptr, nullptr, nullptr, nullptr, state_.p, partials_.p, partials32_.p, ticket_.p,
                               cfg.stop_rule, cfg.er0, cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
             else
-                bicg_chunk<1>(A.view<double>(), BsrView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, r0_.p,
+                bicg_chunk<1>(A.sell<double>(), SellView<float>{}, false, cfg.graph_chunk, A.nb, x, r_.p, r0_.p,
                               pA_.p, pB_.p, yA_.p, yB_.p, e_.p, v_.p, nullptr, nullptr, nullptr, nullptr, nullptr,
                               nullptr, nullptr, nullptr, nullptr, state_.p, partials_.p, partials32_.p, ticket_.p,
                               cfg.stop_rule, cfg.er0, cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
@@ -1025,35 +1125,31 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
     const int64_t n = A.ndof();
     const int g = row_grid(A.nb);
     const int gv = grid_for(n, 256, sm_count() * 8);
-    const uint64_t key = mix_key({3, (uint64_t)cg, (uint64_t)A.bs, (uint64_t)(uintptr_t)A.v32.p,
-                                  (uint64_t)(uintptr_t)x32_.p, (uint64_t)(uintptr_t)r32_.p, (uint64_t)cfg.precond,
-                                  (uint64_t)cfg.graph_chunk, (uint64_t)cfg.itrmax,
-                                  (uint64_t)(cfg.relative_er * 1e18), (uint64_t)(cfg.reliable_delta * 1e18),
-                                  (uint64_t)n});
+    const uint64_t key = graph_key(cg ? 3 : 4, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
         if (graph_) cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
         auto body = [&]() {
             if (cg) {
                 if (A.bs == 3)
-                    cg_chunk<3>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                    cg_chunk<3>(SellView<double>{}, A.sell<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
                                 nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p, z32_.p, pA32_.p, pB32_.p,
                                 q32_.p, dinv32_.p, cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p,
                                 cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
                 else
-                    cg_chunk<1>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                    cg_chunk<1>(SellView<double>{}, A.sell<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
                                 nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p, z32_.p, pA32_.p, pB32_.p,
                                 q32_.p, dinv32_.p, cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p,
                                 cfg.relative_er, cfg.reliable_delta, cfg.itrmax, st);
             } else {
                 if (A.bs == 3)
-                    bicg_chunk<3>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                    bicg_chunk<3>(SellView<double>{}, A.sell<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
                                   nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p,
                                   r032_.p, pA32_.p, pB32_.p, yA32_.p, yB32_.p, e32_.p, v32_.p, state_.p, partials_.p,
                                   partials32_.p, ticket_.p, PFG_STOP_TRUE_RELATIVE, cfg.er0, cfg.relative_er,
                                   cfg.reliable_delta, cfg.itrmax, st);
                 else
-                    bicg_chunk<1>(BsrView<double>{}, A.view<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
+                    bicg_chunk<1>(SellView<double>{}, A.sell<float>(), true, cfg.graph_chunk, A.nb, nullptr, nullptr,
                                   nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, x32_.p, r32_.p,
                                   r032_.p, pA32_.p, pB32_.p, yA32_.p, yB32_.p, e32_.p, v32_.p, state_.p, partials_.p,
                                   partials32_.p, ticket_.p, PFG_STOP_TRUE_RELATIVE, cfg.er0, cfg.relative_er,
@@ -1097,12 +1193,25 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
                                                                state_.p, partials_.p, partials32_.p, ticket_.p,
                                                                first ? 0 : 1);
         } else {
+            // BiCGSTAB restarts fully at a replacement: new shadow residual
+            // r0 = r and p = r.  Keeping the first r0 makes r0.r lose every
+            // FP32 digit once |r| has dropped by many orders.
+            PFG_CUDA(cudaMemsetAsync(pA32_.p, 0, n * sizeof(float), st));
+            PFG_CUDA(cudaMemsetAsync(pB32_.p, 0, n * sizeof(float), st));
+            PFG_CUDA(cudaMemsetAsync(yA32_.p, 0, n * sizeof(float), st));
+            PFG_CUDA(cudaMemsetAsync(yB32_.p, 0, n * sizeof(float), st));
             k_bicg_restart<float><<<g, kThreads, 0, st>>>(n, r32_.p, r032_.p, state_.p, partials_.p, partials32_.p,
-                                                          ticket_.p, first ? 1 : 0, first ? 0 : 1);
+                                                          ticket_.p, 1, 0);
         }
         PFG_CUDA(cudaGetLastError());
         first = false;
         read_state(h, st);
+        if (h.breakdowns > 3 && !h.done) {
+            // repeated FP32 breakdowns with no completed iteration in between
+            res.status = PFG_E_BREAKDOWN;
+            h.status = PFG_E_BREAKDOWN;
+            break;
+        }
         if (cfg.debug != 0)
             fprintf(stderr, "[pfg] mixed iter %d replacement %d |b-Ax|/|b| %.3e\n", h.iter, h.replacements, rel);
         if (h.done) break;
@@ -1142,12 +1251,17 @@ __global__ void k_fill(double *a, int64_t n, double v)
 
 void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
 {
-    PFG_CHECK(kernel >= 0 && kernel <= 2 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel >= 0 && kernel <= 4 && reps > 0, PFG_E_ARG, "bad profile request");
     const int64_t n = A.ndof();
-    const double idx = (double)A.nnzb * 4.0 + (double)(A.nb + 1) * 8.0;  // block columns + row pointers
-    if (kernel != 0 && !A.v32_valid) make_v32(A, st);
+    const double bs2 = (double)(A.bs * A.bs);
+    // algorithmic bytes: values and block columns once, row pointers (int64)
+    // once, source vector once, result once -- padding slots are overhead
+    const double idx = (double)A.nnzb * 4.0 + (double)(A.nb + 1) * 8.0;
+    const bool f64 = kernel == 0 || kernel == 3;
+    if (kernel == 4 && !A.v32_valid) make_v32(A, st);
+    if (kernel <= 2) build_sell(A, f64, !f64, st);
     const int gv = grid_for(n, 256, sm_count() * 8);
-    const int g = row_grid(A.nb);
+    const int gb = row_grid(A.nb);
     DevBuf<double> x64, y64;
     DevBuf<float> x32, y32, p32, q32;
     KState hs;
@@ -1159,35 +1273,49 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
         ticket_.alloc(1);
         PFG_CUDA(cudaMemsetAsync(ticket_.p, 0, sizeof(unsigned), st));
     }
-    partials_.ensure((size_t)g * 4 + 8);
-    partials32_.ensure((size_t)g * 8 + 16);
+    const int g0 = A.bs == 3 ? resident_grid(k_spmv_sell<3, double>, A.ns) : resident_grid(k_spmv_sell<1, double>, A.ns);
+    const int g1 = A.bs == 3 ? resident_grid(k_spmv_sell<3, float>, A.ns) : resident_grid(k_spmv_sell<1, float>, A.ns);
+    const int g2 = A.bs == 3 ? resident_grid(k_cg_spmv<3, float>, A.ns) : resident_grid(k_cg_spmv<1, float>, A.ns);
+    partials_.ensure((size_t)sm_count() * (2048 / kThreads) * 4 + 8);
+    partials32_.ensure((size_t)sm_count() * (2048 / kThreads) * 8 + 16);
     PFG_CUDA(cudaMemcpyAsync(state_.p, &hs, sizeof(KState), cudaMemcpyHostToDevice, st));
     auto launch = [&]() {
-        if (kernel == 0) {
-            if (A.bs == 3) k_spmv<3, double><<<g, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
-            else k_spmv<1, double><<<g, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
-        } else if (kernel == 1) {
-            if (A.bs == 3) k_spmv<3, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, y32.p);
-            else k_spmv<1, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, y32.p);
-        } else {
+        switch (kernel) {
+        case 0:
+            if (A.bs == 3) k_spmv_sell<3, double><<<g0, kThreads, 0, st>>>(A.sell<double>(), x64.p, y64.p);
+            else k_spmv_sell<1, double><<<g0, kThreads, 0, st>>>(A.sell<double>(), x64.p, y64.p);
+            break;
+        case 1:
+            if (A.bs == 3) k_spmv_sell<3, float><<<g1, kThreads, 0, st>>>(A.sell<float>(), x32.p, y32.p);
+            else k_spmv_sell<1, float><<<g1, kThreads, 0, st>>>(A.sell<float>(), x32.p, y32.p);
+            break;
+        case 2:
             if (A.bs == 3)
-                k_cg_spmv<3, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
-                                                            partials_.p, partials32_.p, ticket_.p);
+                k_cg_spmv<3, float><<<g2, kThreads, 0, st>>>(A.sell<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
+                                                             partials_.p, partials32_.p, ticket_.p);
             else
-                k_cg_spmv<1, float><<<g, kThreads, 0, st>>>(A.view<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
-                                                            partials_.p, partials32_.p, ticket_.p);
+                k_cg_spmv<1, float><<<g2, kThreads, 0, st>>>(A.sell<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
+                                                             partials_.p, partials32_.p, ticket_.p);
+            break;
+        case 3:
+            if (A.bs == 3) k_spmv<3, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
+            else k_spmv<1, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
+            break;
+        default:
+            if (A.bs == 3) k_spmv<3, float><<<gb, kThreads, 0, st>>>(A.view<float>(), x32.p, y32.p);
+            else k_spmv<1, float><<<gb, kThreads, 0, st>>>(A.view<float>(), x32.p, y32.p);
         }
     };
-    if (kernel == 0) {
+    if (f64) {
         x64.alloc((size_t)n);
         y64.alloc((size_t)n);
         k_fill<<<gv, 256, 0, st>>>(x64.p, n, 1.0);
-        bytes = (double)A.nnzb * 9.0 * 8.0 + idx + 2.0 * (double)n * 8.0;
+        bytes = (double)A.nnzb * bs2 * 8.0 + idx + 2.0 * (double)n * 8.0;
     } else {
         x32.alloc((size_t)n);
         y32.alloc((size_t)n);
         k_fill<<<gv, 256, 0, st>>>(x32.p, n, 1.0f);
-        bytes = (double)A.nnzb * 9.0 * 4.0 + idx + 2.0 * (double)n * 4.0;
+        bytes = (double)A.nnzb * bs2 * 4.0 + idx + 2.0 * (double)n * 4.0;
         if (kernel == 2) {
             p32.alloc((size_t)n);
             q32.alloc((size_t)n);

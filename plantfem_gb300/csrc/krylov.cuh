@@ -5,6 +5,7 @@
 #pragma once
 
 #include "bsr.cuh"
+#include "sell.cuh"
 
 namespace pfg {
 
@@ -23,7 +24,8 @@ struct KState {
     int parity;            // which of the ping-pong buffers holds the current p
     int status;            // PFG_OK, PFG_E_BREAKDOWN, PFG_W_NOT_CONVERGED
     int replacements;      // mixed: number of FP64 residual replacements
-    int pad[2];
+    int breakdowns;        // mixed BiCGSTAB: FP32 breakdowns since the last completed iteration
+    int pad;
 };
 
 struct KConfig {
@@ -57,14 +59,40 @@ struct DevMatrix {
     DevBuf<double> v64;
     DevBuf<float> v32;
     bool v32_valid = false;
+    // sliced-ELL copy read by the Krylov kernels (sell.cuh), rebuilt on demand
+    int64_t ns = 0;
+    DevBuf<int64_t> sptr;
+    DevBuf<int> scol;
+    DevBuf<double> s64;
+    DevBuf<float> s32;
+    bool sell_pattern = false, s64_valid = false, s32_valid = false;
+
     int64_t ndof() const { return nb * bs; }
+    // v64 changed: every derived copy is stale
+    void values_changed() { v32_valid = s64_valid = s32_valid = false; }
+    // rp/col changed too
+    void pattern_changed()
+    {
+        values_changed();
+        sell_pattern = false;
+    }
     template <typename T>
     BsrView<T> view() const;
+    template <typename T>
+    SellView<T> sell() const;
 };
 template <>
 inline BsrView<double> DevMatrix::view<double>() const { return BsrView<double>{nb, nnzb, rp.p, col.p, v64.p}; }
 template <>
 inline BsrView<float> DevMatrix::view<float>() const { return BsrView<float>{nb, nnzb, rp.p, col.p, v32.p}; }
+template <>
+inline SellView<double> DevMatrix::sell<double>() const { return SellView<double>{nb, ns, sptr.p, scol.p, s64.p}; }
+template <>
+inline SellView<float> DevMatrix::sell<float>() const { return SellView<float>{nb, ns, sptr.p, scol.p, s32.p}; }
+
+// Build (or refresh) the sliced-ELL copy: pattern once, FP64 and/or FP32
+// values when stale.  Implemented in sell.cu.
+void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st);
 
 class Krylov {
   public:
@@ -79,8 +107,9 @@ class Krylov {
     // Grid size used for the row loops (a multiple of the SM count).
     static int row_grid(int64_t nb);
     // Mean ms per launch of one kernel over `reps` launches (CUDA events on st)
-    // and the algorithmic bytes of one launch.  kernel: 0 FP64 SpMV, 1 FP32
-    // SpMV, 2 FP32 CG SpMV with fused direction update.
+    // and the algorithmic bytes of one launch.  kernel: 0 FP64 sliced SpMV,
+    // 1 FP32 sliced SpMV, 2 FP32 CG SpMV with fused direction update (sliced),
+    // 3 FP64 block-row SpMV, 4 FP32 block-row SpMV.
     void profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes);
 
   private:
@@ -90,6 +119,9 @@ class Krylov {
     SolveResult run_bicgstab64(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
     SolveResult run_mixed(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
     void read_state(KState &h, cudaStream_t st);
+    // Hash of everything a captured chunk graph bakes in: every device pointer
+    // its kernels receive and the configuration scalars.
+    uint64_t graph_key(int kind, const DevMatrix &A, const void *x, const KConfig &cfg) const;
     double true_residual(const DevMatrix &A, const double *b, const double *x, double *r, cudaStream_t st);
 
     int64_t n_ = 0;

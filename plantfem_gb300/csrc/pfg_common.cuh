@@ -92,6 +92,12 @@ struct DevBuf {
     {
         if (n < count) alloc(count);
     }
+    // Exactly `count` elements; keeps the allocation (and its address) when
+    // the size is unchanged, so captured CUDA graphs stay valid.
+    void resize(size_t count)
+    {
+        if (n != count) alloc(count);
+    }
     void release()
     {
         if (p) cudaFree(p);
