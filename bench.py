@@ -38,8 +38,9 @@ TOL = 1e-10
 # Iterations the reference algorithm (unpreconditioned bicgstab_CRS_2, FP64,
 # reference stop rule sqrt(rr/rr_1) < 1e-10) needs on lognormal100, measured
 # with this library's FP64 BiCGSTAB on a GB300 (same algorithm and stop rule).
-# The CPU arm times a bounded sample of iterations and scales by this count.
-REF_ITERS_LOGNORMAL100 = None
+# The CPU arm times a bounded sample of iterations and scales by this count
+# (GB300 measurement: 1593 iterations, final |b-Kx|/|b| = 1.3e-9).
+REF_ITERS_LOGNORMAL100 = 1593
 
 
 def peaks():
@@ -195,6 +196,17 @@ def run_ours(args, ws, rank, local):
     ms_f64 = ev0.elapsed_time(ev1) / f64_steps
 
     out_extra = {}
+    if not args.skip_variants:
+        # where the direction update runs: fused into the SpMV gathers or as a
+        # separate streaming pass (auto picks per precision)
+        var = {}
+        for name, prec, um in (("cg_fp64_fused", "fp64", 1), ("cg_fp64_separate", "fp64", 2),
+                               ("cg_mixed_fused", "mixed", 1), ("cg_mixed_separate", "mixed", 2)):
+            x.zero_()
+            iv = s.solve_device(b, x, algorithm="CG", preconditioning="BlockJacobi", precision=prec,
+                                stop_rule="true_relative", update_mode=um)
+            var[name] = {"ms": round(iv["solve_ms"], 2), "iterations": iv["iterations"], "status": iv["status"]}
+        out_extra["update_mode_variants"] = var
     # reference algorithm on the GPU: unpreconditioned BiCGSTAB, reference stop rule
     if not args.skip_bicgstab:
         try:
@@ -224,6 +236,20 @@ def bicgstab_lines(s, b, x):
         "mixed": {"ms": im["solve_ms"], "iterations": im["iterations"], "status": im["status"]},
         "fp64": {"ms": i64["solve_ms"], "iterations": i64["iterations"], "status": i64["status"]},
         "speedup_mixed_vs_fp64": i64["solve_ms"] / im["solve_ms"] if im["solve_ms"] > 0 else None}
+    # right-preconditioned (3x3 block Jacobi) BiCGSTAB, FP64 and mixed with
+    # several residual-replacement intervals
+    pre = {}
+    x.zero_()
+    ip = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning="BlockJacobi", precision="fp64",
+                        stop_rule="true_relative")
+    pre["fp64"] = {"ms": round(ip["solve_ms"], 2), "iterations": ip["iterations"], "status": ip["status"]}
+    for d in (1e-1, 1e-2, 1e-3, 1e-4):
+        x.zero_()
+        iq = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning="BlockJacobi", precision="mixed",
+                            stop_rule="true_relative", reliable_delta=d)
+        pre[f"mixed_delta_{d:g}"] = {"ms": round(iq["solve_ms"], 2), "iterations": iq["iterations"],
+                                     "replacements": iq["replacements"], "status": iq["status"]}
+    out_extra["bicgstab_block_jacobi_true_rel_1e-10"] = pre
     return out_extra
 
 
@@ -358,7 +384,10 @@ def run_reference(args, ws, rank):
         O.bicgstab_crs2(rp, ci, val, b, itrmax=k, relative_er=1e-300, er0=1e-300, atomic=True)
         times.append((time.perf_counter() - t) / k)
     t_it = statistics.median(times)
-    iters = REF_ITERS_LOGNORMAL100
+    if n == N_DEFAULT:
+        iters = REF_ITERS_LOGNORMAL100
+    else:  # small cases: run the reference algorithm to convergence for its count
+        _, _, iters = O.bicgstab_crs2(rp, ci, val, b, atomic=True)
     value = 1.0 / (t_it * iters) if iters else None
     sample = (f"each step: {k} iterations of bicgstab_CRS_2 (oracle C/OpenMP restatement with the per-nonzero "
               f"atomic SpMV of LinearSolverClass.f90:3766-3774) on lognormal{n}; {t_it * 1e3:.1f} ms/iteration "
@@ -395,6 +424,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-bicgstab", action="store_true")
+    ap.add_argument("--skip-variants", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -67,7 +67,8 @@ typedef struct pfg_solve_opts {
     double reliable_delta;   /* mixed: replace the FP32 residual by the FP64 one whenever it fell
                                 by this factor since the last replacement; default 0.1 */
     int32_t debug;           /* FEMSolver_%debug: print the residual per graph chunk */
-    int32_t reserved;
+    int32_t update_mode;     /* 0 auto, 1 vector updates fused into the SpMV gathers,
+                                2 separate streaming passes (see krylov.cu) */
 } pfg_solve_opts;
 
 typedef struct pfg_info {

@@ -35,7 +35,7 @@ class SolveOpts(C.Structure):
     _fields_ = [("algorithm", C.c_int32), ("precision", C.c_int32), ("precond", C.c_int32),
                 ("stop_rule", C.c_int32), ("itrmax", C.c_int32), ("graph_chunk", C.c_int32),
                 ("er0", C.c_double), ("relative_er", C.c_double), ("reliable_delta", C.c_double),
-                ("debug", C.c_int32), ("reserved", C.c_int32)]
+                ("debug", C.c_int32), ("update_mode", C.c_int32)]
 
 
 class Info(C.Structure):

@@ -125,6 +125,7 @@ KConfig to_config(const pfg_solve_opts *o)
     c.reliable_delta = o->reliable_delta;
     c.graph_chunk = o->graph_chunk;
     c.debug = o->debug;
+    c.fuse = o->update_mode == 1 ? 1 : (o->update_mode == 2 ? 0 : -1);
     return c;
 }
 

@@ -37,6 +37,7 @@ struct KConfig {
     double er0, relative_er, reliable_delta;
     int graph_chunk;
     int debug;
+    int fuse;  // 1: vector updates ride in the SpMV gathers, 0: separate streaming passes
 };
 
 struct SolveResult {
@@ -127,9 +128,9 @@ class Krylov {
     int64_t n_ = 0;
     int bs_ = 3;
     // FP64 work vectors
-    DevBuf<double> r_, r0_, z_, pA_, pB_, q_, yA_, yB_, e_, v_, dinv_;
+    DevBuf<double> r_, r0_, z_, pA_, pB_, q_, yA_, yB_, e_, v_, dinv_, ph_, eh_;
     // FP32 work vectors
-    DevBuf<float> r32_, r032_, z32_, pA32_, pB32_, q32_, yA32_, yB32_, e32_, v32_, x32_, dinv32_;
+    DevBuf<float> r32_, r032_, z32_, pA32_, pB32_, q32_, yA32_, yB32_, e32_, v32_, x32_, dinv32_, ph32_, eh32_;
     DevBuf<double> partials_;
     DevBuf<float> partials32_;
     DevBuf<unsigned int> ticket_;

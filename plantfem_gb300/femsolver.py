@@ -179,7 +179,7 @@ class FEMSolver:
                                   0.0 if FixValue is None else float(FixValue)))
 
     # ------------------------------------------------------------- solving
-    def _opts(self, algorithm, precision, preconditioning, stop_rule):
+    def _opts(self, algorithm, precision, preconditioning, stop_rule, update_mode=0, reliable_delta=None):
         alg = {"BiCGSTAB": N.ALG_BICGSTAB, "CG": N.ALG_CG}[algorithm or "BiCGSTAB"]
         prec = {"fp64": N.PREC_FP64, "FP64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
         pc = {None: N.PC_NONE, "None": N.PC_NONE, "PointJacobi": N.PC_JACOBI, "Jacobi": N.PC_JACOBI,
@@ -187,11 +187,16 @@ class FEMSolver:
         if stop_rule is None:
             stop_rule = "reference" if prec == N.PREC_FP64 else "true_relative"
         sr = {"reference": N.STOP_REFERENCE, "true_relative": N.STOP_TRUE_RELATIVE}[stop_rule]
-        return N.default_opts(algorithm=alg, precision=prec, precond=pc, stop_rule=sr, itrmax=int(self.itrmax),
-                              er0=float(self.er0), relative_er=float(self.relative_er), debug=int(bool(self.debug)))
+        um = {0: 0, "auto": 0, 1: 1, "fused": 1, 2: 2, "separate": 2}[update_mode]
+        o = N.default_opts(algorithm=alg, precision=prec, precond=pc, stop_rule=sr, itrmax=int(self.itrmax),
+                           er0=float(self.er0), relative_er=float(self.relative_er), debug=int(bool(self.debug)),
+                           update_mode=um)
+        if reliable_delta is not None:
+            o.reliable_delta = float(reliable_delta)
+        return o
 
     def solve(self, algorithm: str | None = None, preconditioning: str | None = None, x0=None,
-              precision: str = "fp64", stop_rule: str | None = None) -> np.ndarray:
+              precision: str = "fp64", stop_rule: str | None = None, update_mode=0) -> np.ndarray:
         """x = FEMSolver_%solve([algorithm], [preconditioning], [x0]) (FEMSolverClass.f90:1697-1825).
 
         Defaults reproduce the reference: unpreconditioned BiCGSTAB in FP64 with
@@ -199,7 +204,7 @@ class FEMSolver:
         ``precision="mixed"`` select the GB300 forms.  Breakdown raises
         (the reference stops); itrmax is reported in ``last_info``.
         """
-        opts = self._opts(algorithm, precision, preconditioning, stop_rule)
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode)
         n = self.ndof()
         x = np.zeros(n)
         xi = None if x0 is None else _f64(x0)
@@ -209,10 +214,10 @@ class FEMSolver:
         return x
 
     def solve_device(self, b, x, algorithm="CG", preconditioning="BlockJacobi", precision="mixed",
-                     stop_rule=None, stream=None):
+                     stop_rule=None, stream=None, update_mode=0, reliable_delta=None):
         """Solve with the already-eliminated matrix on device tensors b -> x
         (x holds x0).  ``b`` and ``x`` are float64 CUDA tensors."""
-        opts = self._opts(algorithm, precision, preconditioning, stop_rule)
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, reliable_delta)
         info = N.Info()
         if stream is None:
             _torch_sync()  # the library works on its own stream: order after the caller's writes

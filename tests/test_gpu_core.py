@@ -187,9 +187,12 @@ def test_solve_golden_cube4(cuda, algorithm, precision, pc):
     assert _rel(x, g["x"]) <= 1e-8
 
 
+@pytest.mark.parametrize("update_mode", [1, 2])
 @pytest.mark.parametrize("algorithm,precision,pc", [("CG", "fp64", "BlockJacobi"), ("CG", "mixed", "BlockJacobi"),
-                                                    ("BiCGSTAB", "mixed", None), ("BiCGSTAB", "fp64", None)])
-def test_solve_vs_fp64_oracle(cuda, algorithm, precision, pc):
+                                                    ("BiCGSTAB", "mixed", None), ("BiCGSTAB", "fp64", None),
+                                                    ("BiCGSTAB", "mixed", "BlockJacobi"),
+                                                    ("BiCGSTAB", "fp64", "Jacobi")])
+def test_solve_vs_fp64_oracle(cuda, algorithm, precision, pc, update_mode):
     """Displacement within 1e-8 of the FP64 oracle solved to 1e-12."""
     p = problems.lognormal(12)
     dom = p["domain"]
@@ -201,7 +204,8 @@ def test_solve_vs_fp64_oracle(cuda, algorithm, precision, pc):
     s.setRHS(p["rhs"])
     s.fix(1, p["fix_ids"], FixValue=0.0)
     s.relative_er = 1e-12
-    x = s.solve(algorithm=algorithm, preconditioning=pc, precision=precision, stop_rule="true_relative")
+    x = s.solve(algorithm=algorithm, preconditioning=pc, precision=precision, stop_rule="true_relative",
+                update_mode=update_mode)
     assert s.last_info["status"] == 0, s.last_info
     assert _rel(x, xo) <= 1e-8, (_rel(x, xo), s.last_info)
 
