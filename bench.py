@@ -186,6 +186,7 @@ def run_ours(args, ws, rank, local):
     err_mixed = float(torch.linalg.norm(x - x_ref) / torch.linalg.norm(x_ref))
     mixed_info = infos[-1]
 
+    _progress(f"timed mixed solves done: {ms_step:.1f} ms/solve")
     # plain FP64 GPU path (same algorithm, preconditioner and stop rule)
     f64_steps = max(1, min(args.steps, 3))
     solve_once("fp64")
@@ -221,36 +222,74 @@ def run_ours(args, ws, rank, local):
 def bicgstab_lines(s, b, x):
     """The reference algorithm (unpreconditioned BiCGSTAB) on the GPU: FP64 with
     the reference stop rule, then FP64 and mixed to the true 1e-10 residual."""
-    out_extra = {}
-    x.zero_()
-    ib = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64", stop_rule="reference")
-    out_extra["bicgstab_fp64_reference_rule"] = {"iterations": ib["iterations"], "ms": ib["solve_ms"],
-                                                 "rel_residual": ib["rel_residual"], "status": ib["status"]}
-    x.zero_()
-    im = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="mixed",
-                        stop_rule="true_relative")
-    x.zero_()
-    i64 = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=None, precision="fp64",
-                         stop_rule="true_relative")
-    out_extra["bicgstab_true_rel_1e-10"] = {
-        "mixed": {"ms": im["solve_ms"], "iterations": im["iterations"], "status": im["status"]},
-        "fp64": {"ms": i64["solve_ms"], "iterations": i64["iterations"], "status": i64["status"]},
-        "speedup_mixed_vs_fp64": i64["solve_ms"] / im["solve_ms"] if im["solve_ms"] > 0 else None}
-    # right-preconditioned (3x3 block Jacobi) BiCGSTAB, FP64 and mixed with
-    # several residual-replacement intervals
-    pre = {}
-    x.zero_()
-    ip = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning="BlockJacobi", precision="fp64",
-                        stop_rule="true_relative")
-    pre["fp64"] = {"ms": round(ip["solve_ms"], 2), "iterations": ip["iterations"], "status": ip["status"]}
-    for d in (1e-1, 1e-2, 1e-3, 1e-4):
+    def run(**kw):
         x.zero_()
-        iq = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning="BlockJacobi", precision="mixed",
-                            stop_rule="true_relative", reliable_delta=d)
-        pre[f"mixed_delta_{d:g}"] = {"ms": round(iq["solve_ms"], 2), "iterations": iq["iterations"],
-                                     "replacements": iq["replacements"], "status": iq["status"]}
-    out_extra["bicgstab_block_jacobi_true_rel_1e-10"] = pre
-    return out_extra
+        try:
+            i = s.solve_device(b, x, algorithm="BiCGSTAB", **kw)
+            return {"ms": round(i["solve_ms"], 2), "iterations": i["iterations"], "replacements": i["replacements"],
+                    "rel_residual": i["rel_residual"], "status": i["status"]}
+        except Exception as e:  # reported per variant, not fatal
+            return {"error": str(e)}
+
+    itr = s.itrmax
+    s.itrmax = 20000  # bound every variant (a diverging one stops here)
+    try:
+        out = {"reference_rule_fp64": run(preconditioning=None, precision="fp64", stop_rule="reference")}
+        _progress("bicgstab reference rule done")
+        for pc in (None, "BlockJacobi"):
+            tag = "block_jacobi" if pc else "none"
+            out[f"{tag}_fp64"] = run(preconditioning=pc, precision="fp64", stop_rule="true_relative")
+            for d in (1e-1, 3e-2):
+                out[f"{tag}_mixed_delta_{d:g}"] = run(preconditioning=pc, precision="mixed",
+                                                      stop_rule="true_relative", reliable_delta=d)
+            _progress(f"bicgstab {tag} done")
+    finally:
+        s.itrmax = itr
+    bj = out.get("block_jacobi_fp64", {}), out.get("block_jacobi_mixed_delta_0.1", {})
+    if "ms" in bj[0] and "ms" in bj[1]:
+        out["speedup_mixed_vs_fp64_block_jacobi"] = round(bj[0]["ms"] / bj[1]["ms"], 3)
+    return {"bicgstab_fp64_reference_rule": out["reference_rule_fp64"], "bicgstab_variants_rel_1e-10": out}
+
+
+def _progress(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def modal_lines(n=60, nev=20, block=24, tol=1e-8):
+    """Modal analysis (LOBPCG, FEMSolver_%eig): cantilever n^3 (one x face
+    fixed), consistent mass rho=1e3; lowest nev pairs, block 24, tol 1e-8;
+    FP64 vs mixed (FP32 phase, then FP64)."""
+    from plantfem_gb300 import FEMSolver, problems
+    p = problems.cantilever(n)
+    s = FEMSolver()
+    s.setDomain(p["domain"])
+    s.setCRS(3)
+    s.assembleMass(p["rho"])
+    s.keepThisMatrixAs("B")
+    s.zeros()
+    s.assembleStiffness(p["E"], p["nu"])
+    s.keepThisMatrixAs("A")
+    s.fix_eig(p["fix_ids"])
+    s.LOBPCG_TOL = tol
+    s.LOBPCG_MAX_ITR = 3000
+    out = {"workload": f"cantilever{n}: {3 * p['domain'].nn()} DOF, {len(p['fix_ids'])} fixed, nev {nev}, "
+                       f"block {block}, tol {tol:g}"}
+    lams = {}
+    for prec in ("fp64", "mixed"):
+        try:
+            lam, _ = s.eig(nev, block_size=block, precision=prec, eigen_vectors=False)
+            i = s.last_info
+            lams[prec] = lam
+            out[prec] = {"ms": round(i["solve_ms"], 1), "iterations": i["iterations"],
+                         "fp32_iterations": i["replacements"], "max_rel_residual": i["rel_residual"],
+                         "status": i["status"], "lambda_1": lam[0], "lambda_nev": lam[-1]}
+        except Exception as e:
+            out[prec] = {"error": str(e)}
+    if len(lams) == 2:
+        out["max_rel_eigenvalue_diff"] = float(np.abs(lams["mixed"] - lams["fp64"]).max() / np.abs(lams["fp64"]).max())
+        out["speedup_mixed_vs_fp64"] = round(out["fp64"]["ms"] / out["mixed"]["ms"], 3)
+    s.remove()
+    return out
 
 
 def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_mixed, ms_step, value, f64_infos,
@@ -273,6 +312,7 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
                 "frac": round(dom_k["GBs"] / peak, 4), "traffic": None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk else "fallback 6800 GB/s"}
 
+    _progress("kernel profiles done")
     # end to end through the C ABI plug-in with host (pinned) CRS arrays
     e2e = None
     if not args.skip_e2e:
@@ -299,11 +339,14 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
                "rel_err_vs_fp64": float(np.linalg.norm(xn - x64_host) / np.linalg.norm(x64_host))}
         del rp_p, ci_p, val_p
 
+    _progress("end-to-end done")
     # CPU baseline: the oracle's bicgstab_CRS_2 restatement on the host cores
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
         cpu = cpu_baseline_sample(s, out_extra.get("bicgstab_fp64_reference_rule", {}).get("iterations"))
 
+    if args.modal and rank == 0:
+        out_extra["modal_lobpcg"] = modal_lines(args.modal_n)
     launches = int(sum(i["kernel_launches"] for i in infos))
     line = {
         "metric": "solves/s of the 3,090,903-DOF hex8 elasticity solve at 1e-10 relative residual "
@@ -425,6 +468,8 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-bicgstab", action="store_true")
     ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--modal", action="store_true", help="also run the LOBPCG modal analysis (FP64 vs mixed)")
+    ap.add_argument("--modal-n", type=int, default=60)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -164,6 +164,44 @@ int pfg_fix(pfg_solver *h, int64_t n, const int32_t *ids, const double *values, 
  * x_out receives n values; info may be NULL. */
 int pfg_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *x0, double *x_out, pfg_info *info);
 
+/* ------------------------------------------------------------- eigenproblem */
+/* FEMSolver_%keepThisMatrixAs(As) (FEMSolverClass.f90:1544-1604): copy the
+ * working matrix into a named slot ("A" = stiffness, "B" = mass for eig); at
+ * most 10 names, an existing name is overwritten. */
+int pfg_keep_this_matrix_as(pfg_solver *h, const char *name);
+
+/* FEMSolver_%fix_eig(IDs) (FEMSolverClass.f90:1607-1628): 1-based DOF ids whose
+ * amplitude is zero in eig; accumulated, duplicates ignored. */
+int pfg_fix_eig(pfg_solver *h, int64_t n, const int32_t *ids);
+
+#define PFG_EIG_STOP_REFERENCE 0 /* max|R| / max|R at iteration 1| < tol, SparseClass.f90:2218-2234 */
+#define PFG_EIG_STOP_RESIDUAL 1  /* every wanted pair |K x - lambda M x| / (lambda |M x|) < tol */
+
+typedef struct pfg_eig_opts {
+    int32_t block_size;      /* LOBPCG block k >= num_eigen (<= 32); 0: num_eigen as the reference */
+    int32_t max_itr;         /* FEMSolver_%LOBPCG_MAX_ITR, default 100000 */
+    double tol;              /* FEMSolver_%LOBPCG_TOL, default 1e-6 */
+    int32_t precision;       /* PFG_PREC_FP64 or PFG_PREC_MIXED (FP32 phase, then FP64) */
+    int32_t precond;         /* PFG_PC_BLOCK_JACOBI (default) or PFG_PC_JACOBI / PFG_PC_NONE */
+    int32_t stop_rule;       /* PFG_EIG_STOP_*, default PFG_EIG_STOP_RESIDUAL */
+    int32_t debug;
+    uint64_t seed;           /* start block (the reference's random%randn is unseeded) */
+    double tol_fp32;         /* mixed: FP32 phase ends at this relative residual, default 1e-4 */
+} pfg_eig_opts;
+
+void pfg_eig_opts_default(pfg_eig_opts *opts);
+
+/* FEMSolver_%eig(num_eigen, eigen_value, eigen_vectors) with use_LOBPCG
+ * (FEMSolverClass.f90:1384-1541 -> LOBPCG_CRS SparseClass.f90:2008-2239):
+ * lowest num_eigen pairs of A x = lambda B x (the slots kept as "A" and "B")
+ * with the fix_eig DOFs removed.  eigen_value[num_eigen] ascending;
+ * eigen_vectors (may be NULL): ndof x num_eigen column-major, B-orthonormal,
+ * zero at the fixed DOFs (as the reference scatters them back, :1498-1539).
+ * info->iterations = LOBPCG iterations, info->rel_residual = largest relative
+ * residual of the wanted pairs. */
+int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *eigen_value, double *eigen_vectors,
+            pfg_info *info);
+
 /* ------------------------------------------------ reference-signature plug-ins */
 /* crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector, n, col_size)
  * (SparseClass-c.c:131-143, bound at SparseClass.f90:38-51): new_vector += A *

@@ -38,6 +38,15 @@ class SolveOpts(C.Structure):
                 ("debug", C.c_int32), ("update_mode", C.c_int32)]
 
 
+class EigOpts(C.Structure):
+    _fields_ = [("block_size", C.c_int32), ("max_itr", C.c_int32), ("tol", C.c_double), ("precision", C.c_int32),
+                ("precond", C.c_int32), ("stop_rule", C.c_int32), ("debug", C.c_int32), ("seed", C.c_uint64),
+                ("tol_fp32", C.c_double)]
+
+
+EIG_STOP_REFERENCE, EIG_STOP_RESIDUAL = 0, 1
+
+
 class Info(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("replacements", C.c_int32),
                 ("kernel_launches", C.c_int32), ("rel_residual", C.c_double), ("iter_residual", C.c_double),
@@ -83,6 +92,10 @@ SIGNATURES = {
     "pfg_dev_spmv": (C.c_int, [_P, _P, _P, _P]),
     "pfg_dev_solve": (C.c_int, [_P, C.POINTER(SolveOpts), _P, _P, C.POINTER(Info), _P]),
     "pfg_profile_kernel": (C.c_int, [_P, _i32, _i32, C.POINTER(_d), C.POINTER(_d)]),
+    "pfg_keep_this_matrix_as": (C.c_int, [_P, C.c_char_p]),
+    "pfg_fix_eig": (C.c_int, [_P, _i64, _P]),
+    "pfg_eig_opts_default": (None, [C.POINTER(EigOpts)]),
+    "pfg_eig": (C.c_int, [_P, C.POINTER(EigOpts), _i32, _P, _P, C.POINTER(Info)]),
 }
 
 _LIB = None

@@ -639,3 +639,129 @@ extern "C" int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, d
         h->kry.profile(h->K, kernel, reps, h->st, *ms_per_launch, *bytes_per_launch);
     });
 }
+
+// ------------------------------------------------------------- eigenproblem
+#include "lobpcg.cuh"
+
+namespace {
+
+void copy_matrix(const DevMatrix &src, DevMatrix &dst, cudaStream_t st)
+{
+    dst.bs = src.bs;
+    dst.nb = src.nb;
+    dst.nnzb = src.nnzb;
+    dst.rp.resize(src.rp.n);
+    dst.col.resize(src.col.n);
+    dst.v64.resize(src.v64.n);
+    PFG_CUDA(cudaMemcpyAsync(dst.rp.p, src.rp.p, src.rp.bytes(), cudaMemcpyDeviceToDevice, st));
+    PFG_CUDA(cudaMemcpyAsync(dst.col.p, src.col.p, src.col.bytes(), cudaMemcpyDeviceToDevice, st));
+    PFG_CUDA(cudaMemcpyAsync(dst.v64.p, src.v64.p, src.v64.bytes(), cudaMemcpyDeviceToDevice, st));
+    dst.pattern_changed();
+}
+
+DevMatrix *find_slot(pfg_solver *h, const std::string &name)
+{
+    for (auto &kv : h->stack)
+        if (kv.first == name) return &kv.second;
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+void pfg_eig_opts_default(pfg_eig_opts *o)
+{
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->block_size = 0;
+    o->max_itr = 100000;
+    o->tol = 1.0e-6;
+    o->precision = PFG_PREC_FP64;
+    o->precond = PFG_PC_BLOCK_JACOBI;
+    o->stop_rule = PFG_EIG_STOP_RESIDUAL;
+    o->seed = 1;
+    o->tol_fp32 = 1.0e-4;
+}
+
+int pfg_keep_this_matrix_as(pfg_solver *h, const char *name)
+{
+    return guard([&] {
+        need(h && name, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "keepThisMatrixAs before setCRS");
+        flush_pending(h);
+        DevMatrix *slot = find_slot(h, name);
+        if (!slot) {
+            need(h->stack.size() < 10, PFG_E_ARG, "keepThisMatrixAs: more than 10 named matrices");
+            h->stack.emplace_back(std::string(name), DevMatrix());
+            slot = &h->stack.back().second;
+        }
+        copy_matrix(h->K, *slot, h->st);
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_fix_eig(pfg_solver *h, int64_t n, const int32_t *ids)
+{
+    return guard([&] {
+        need(h && (ids || n == 0), PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        for (int64_t i = 0; i < n; ++i) h->fix_eig_ids.push_back(ids[i]);
+        std::sort(h->fix_eig_ids.begin(), h->fix_eig_ids.end());
+        h->fix_eig_ids.erase(std::unique(h->fix_eig_ids.begin(), h->fix_eig_ids.end()), h->fix_eig_ids.end());
+    });
+}
+
+int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *eigen_value, double *eigen_vectors,
+            pfg_info *info)
+{
+    EigResult r;
+    const int rc = guard([&] {
+        need(h && eigen_value && num_eigen >= 1, PFG_E_ARG, "bad eig arguments");
+        std::lock_guard<std::mutex> lk(h->mu);
+        DevMatrix *A = find_slot(h, "A"), *B = find_slot(h, "B");
+        need(A && B, PFG_E_STATE, "eig needs matrices kept as \"A\" and \"B\" (keepThisMatrixAs)");
+        need(A->nb == B->nb && A->bs == B->bs, PFG_E_ARG, "A and B differ in size or block structure");
+        pfg_eig_opts d;
+        pfg_eig_opts_default(&d);
+        if (!opts) opts = &d;
+        EigConfig cfg;
+        cfg.nev = num_eigen;
+        cfg.block = opts->block_size > 0 ? opts->block_size : num_eigen;
+        cfg.max_itr = opts->max_itr > 0 ? opts->max_itr : 100000;
+        cfg.tol = opts->tol > 0 ? opts->tol : 1e-6;
+        cfg.precision = opts->precision;
+        cfg.precond = opts->precond;
+        cfg.stop_rule = opts->stop_rule;
+        cfg.seed = opts->seed;
+        cfg.tol_fp32 = opts->tol_fp32 > 0 ? opts->tol_fp32 : 1e-4;
+        cfg.debug = opts->debug;
+        const int64_t n = A->ndof();
+        std::vector<uint8_t> mask((size_t)n, 0);
+        for (int id : h->fix_eig_ids)
+            if (id >= 1 && id <= n) mask[(size_t)id - 1] = 1;
+        DevBuf<uint8_t> dmask((size_t)n);
+        PFG_CUDA(cudaMemcpyAsync(dmask.p, mask.data(), n, cudaMemcpyHostToDevice, h->st));
+        DevBuf<double> X(eigen_vectors ? (size_t)n * num_eigen : 0);
+        r = lobpcg_solve(*A, *B, dmask.p, cfg, eigen_value, eigen_vectors ? X.p : nullptr, h->st);
+        if (eigen_vectors)
+            PFG_CUDA(cudaMemcpyAsync(eigen_vectors, X.p, (size_t)n * num_eigen * sizeof(double), cudaMemcpyDeviceToHost,
+                                     h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        if (info) {
+            info->status = r.status;
+            info->iterations = r.iterations;
+            info->replacements = r.iterations_fp32;
+            info->kernel_launches = r.launches;
+            info->rel_residual = r.max_rel_residual;
+            info->iter_residual = r.max_rel_residual;
+            info->solve_ms = r.ms;
+        }
+    });
+    if (rc != PFG_OK) return rc;
+    if (r.status == PFG_W_NOT_CONVERGED) set_last_error("[ERROR] LOBPCG NOT CONVERGED (LOBPCG_MAX_ITR reached)");
+    return r.status;
+}
+
+}  // extern "C"

@@ -431,8 +431,14 @@ __global__ void __launch_bounds__(kThreads)
         S->parity ^= 1;
         const double rho_n = (double)tot[0], rr = (double)tot[1];
         if (!finite_d(rho_n) || !finite_d(rr)) {
-            S->status = PFG_E_NONFINITE;
-            S->done = 1;
+            if (sizeof(T) == 8) {
+                S->status = PFG_E_NONFINITE;
+                S->done = 1;
+            } else {  // FP32 overflow: restart from the FP64 residual
+                S->need_update = 1;
+                S->breakdowns += 1;
+                S->poisoned = 1;
+            }
             return;
         }
         if (sizeof(T) == 8) {
@@ -647,8 +653,13 @@ __global__ void __launch_bounds__(kThreads)
         S->parity ^= 1;
         const double rr = (double)tot[0], c1n = (double)tot[1];
         if (!finite_d(rr) || !finite_d(c1n)) {
-            S->status = PFG_E_NONFINITE;
-            S->done = 1;
+            if (f64) {
+                S->status = PFG_E_NONFINITE;
+                S->done = 1;
+            } else {
+                bicg_breakdown(S, false);  // FP32 overflow: restart from the FP64 residual
+                S->poisoned = 1;
+            }
             return;
         }
         if (f64) {
@@ -675,7 +686,12 @@ __global__ void __launch_bounds__(kThreads)
             const float rn = sqrtf((float)rr);
             S->rr32 = (float)rr;
             S->rmax32 = fmaxf(S->rmax32, rn);
-            if ((double)rn < delta * (double)S->rmax32 || (double)rn <= tol * sqrt(S->bb)) {
+            S->rmin32 = fminf(S->rmin32, rn);
+            // replace on progress (delta), at the tolerance, or when the FP32
+            // recursion diverges (1000x above its minimum since the last
+            // replacement) before it can spoil the FP64 solution
+            if ((double)rn < delta * (double)S->rmax32 || (double)rn <= tol * sqrt(S->bb) ||
+                rn > 1000.f * S->rmin32) {
                 S->need_update = 1;
             } else {
                 const float c2c3 = S->c2_32 * S->c3_32;
@@ -839,16 +855,17 @@ __global__ void __launch_bounds__(kThreads)
     k_bicg_restart(int64_t n, const T *__restrict__ r, T *__restrict__ r0, KState *S, double *pd, float *pf,
                    unsigned *ticket, int set_r0, int keep_direction)
 {
-    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    typename Acc<T>::type acc[3] = {Acc<T>::zero(), Acc<T>::zero(), Acc<T>::zero()};
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const T ri = r[i];
         if (set_r0) r0[i] = ri;
         const T r0i = set_r0 ? ri : r0[i];
         Acc<T>::add(acc[0], r0i, ri);
         Acc<T>::add(acc[1], ri, ri);
+        Acc<T>::add(acc[2], r0i, r0i);
     }
-    T tot[2];
-    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+    T tot[3];
+    if (grid_total<3>(acc, pd, pf, ticket, tot)) {
         if (sizeof(T) == 8) {
             S->c1 = (double)tot[0];
             S->rr = (double)tot[1];
@@ -861,7 +878,9 @@ __global__ void __launch_bounds__(kThreads)
             if (!keep_direction) S->c3_32 = 0.f;
             S->c1_32 = c1n;
             S->rr32 = tot[1];
+            S->r0r0_32 = tot[2];
             S->rmax32 = sqrtf(tot[1]);
+            S->rmin32 = S->rmax32;
             S->need_update = 0;
         }
     }
@@ -993,6 +1012,16 @@ void Krylov::prepare(const DevMatrix &A, const KConfig &cfg, cudaStream_t st)
     if (!state_.p) state_.alloc(1);
     PFG_CUDA(cudaMemsetAsync(state_.p, 0, sizeof(KState), st));
     (void)st;
+}
+
+void block_jacobi_inverse(const DevMatrix &A, int pc, double *d64, cudaStream_t st)
+{
+    const int g = grid_for(A.nb, 256, sm_count() * 8);
+    if (A.bs == 3)
+        k_precond<3><<<g, 256, 0, st>>>(A.view<double>(), pc, d64, nullptr);
+    else
+        k_precond<1><<<g, 256, 0, st>>>(A.view<double>(), pc, d64, nullptr);
+    PFG_CUDA(cudaGetLastError());
 }
 
 void Krylov::build_precond(const DevMatrix &A, int precond, bool fp32, cudaStream_t st)
@@ -1389,9 +1418,16 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
     for (;;) {
         // residual replacement: x64 += x32; r64 = b - A64 x64; r32 = r64
         if (!first) {
-            k_fold<<<gv, 256, 0, st>>>(n, x, x32_.p);
-            PFG_CUDA(cudaGetLastError());
-            ++launches_;
+            if (h.poisoned) {
+                // the last FP32 update overflowed: keep x64, drop the correction
+                PFG_CUDA(cudaMemsetAsync(x32_.p, 0, n * sizeof(float), st));
+                const int zero = 0;
+                PFG_CUDA(cudaMemcpyAsync(&state_.p->poisoned, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+            } else {
+                k_fold<<<gv, 256, 0, st>>>(n, x, x32_.p);
+                PFG_CUDA(cudaGetLastError());
+                ++launches_;
+            }
         }
         const double rel = true_residual(A, b, x, r_.p, st);
         res.rel_residual = rel;
@@ -1408,15 +1444,29 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
                                                                state_.p, partials_.p, partials32_.p, ticket_.p,
                                                                first ? 0 : 1);
         } else {
-            // BiCGSTAB restarts fully at a replacement: new shadow residual
-            // r0 = r and p = r.  Keeping the first r0 makes r0.r lose every
-            // FP32 digit once |r| has dropped by many orders.
-            PFG_CUDA(cudaMemsetAsync(pA32_.p, 0, n * sizeof(float), st));
-            PFG_CUDA(cudaMemsetAsync(pB32_.p, 0, n * sizeof(float), st));
-            PFG_CUDA(cudaMemsetAsync(yA32_.p, 0, n * sizeof(float), st));
-            PFG_CUDA(cudaMemsetAsync(yB32_.p, 0, n * sizeof(float), st));
-            k_bicg_restart<float><<<g, kThreads, 0, st>>>(n, r32_.p, r032_.p, state_.p, partials_.p, partials32_.p,
-                                                          ticket_.p, 1, 0);
+            // Keep the search direction and the shadow residual r0 while r0.r
+            // still carries FP32 digits (|cos(r0, r)| > 1e-3); otherwise, or
+            // after a breakdown, restart with r0 = r and p = r.  Keeping the
+            // first r0 for good makes r0.r lose every FP32 digit once |r| has
+            // dropped by many orders.
+            bool full = first || h.breakdowns > 0;
+            if (!full) {
+                k_bicg_restart<float><<<g, kThreads, 0, st>>>(n, r32_.p, r032_.p, state_.p, partials_.p,
+                                                              partials32_.p, ticket_.p, 0, 1);
+                PFG_CUDA(cudaGetLastError());
+                ++launches_;
+                read_state(h, st);
+                const double den = std::sqrt((double)h.rr32 * (double)h.r0r0_32);
+                full = !(den > 0.0 && std::fabs((double)h.c1_32) > 1e-3 * den);
+            }
+            if (full) {
+                PFG_CUDA(cudaMemsetAsync(pA32_.p, 0, n * sizeof(float), st));
+                PFG_CUDA(cudaMemsetAsync(pB32_.p, 0, n * sizeof(float), st));
+                PFG_CUDA(cudaMemsetAsync(yA32_.p, 0, n * sizeof(float), st));
+                PFG_CUDA(cudaMemsetAsync(yB32_.p, 0, n * sizeof(float), st));
+                k_bicg_restart<float><<<g, kThreads, 0, st>>>(n, r32_.p, r032_.p, state_.p, partials_.p,
+                                                              partials32_.p, ticket_.p, 1, 0);
+            }
         }
         PFG_CUDA(cudaGetLastError());
         first = false;

@@ -16,7 +16,7 @@ struct KState {
     // FP64 recurrences
     double rho, rho_prev, alpha, beta, pq, rr, bb, rr1, c1, c2, c3, ev, vv;
     // FP32 recurrences of the mixed-precision inner iteration
-    float rho32, alpha32, beta32, rr32, c1_32, c2_32, c3_32, rmax32;
+    float rho32, alpha32, beta32, rr32, c1_32, c2_32, c3_32, rmax32, rmin32, r0r0_32;
     double true_rr;        // |b - A x|^2 in FP64 at the last residual replacement
     int iter;              // inner iterations done
     int done;              // 1 = stop (converged, breakdown or itrmax)
@@ -25,7 +25,7 @@ struct KState {
     int status;            // PFG_OK, PFG_E_BREAKDOWN, PFG_W_NOT_CONVERGED
     int replacements;      // mixed: number of FP64 residual replacements
     int breakdowns;        // mixed BiCGSTAB: FP32 breakdowns since the last completed iteration
-    int pad;
+    int poisoned;          // mixed: an FP32 update produced a non-finite value; drop x32
 };
 
 struct KConfig {

@@ -1,0 +1,836 @@
+// lobpcg.cu -- block LOBPCG on the device (see lobpcg.cuh).
+#include <algorithm>
+#include <cmath>
+#include <type_traits>
+#include <vector>
+
+#include "lobpcg.cuh"
+
+namespace pfg {
+
+// ===================================================================== host
+// Symmetric eigensolver for the small Rayleigh-Ritz problems: Householder
+// reduction to tridiagonal form with accumulated transformations, then the
+// implicit QL iteration with shifts (Bowdler, Martin, Reinsch & Wilkinson,
+// Numer. Math. 11 (1968), the method of EISPACK's tql2).  A is n x n column-
+// major, replaced by the eigenvectors; w receives the eigenvalues ascending.
+static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
+{
+    auto a = [&](int i, int j) -> double & { return A[(size_t)j * n + i]; };
+    std::vector<double> Q((size_t)n * n, 0.0), d(n), e(n, 0.0), v(n), p(n), q(n);
+    for (int i = 0; i < n; ++i) Q[(size_t)i * n + i] = 1.0;
+    // Householder: zero column j below the subdiagonal
+    for (int j = 0; j + 2 < n; ++j) {
+        double alpha = 0.0;
+        for (int i = j + 1; i < n; ++i) alpha += a(i, j) * a(i, j);
+        alpha = std::sqrt(alpha);
+        if (alpha == 0.0) continue;
+        if (a(j + 1, j) > 0) alpha = -alpha;
+        // v = x - alpha e1 on rows j+1..n-1
+        for (int i = 0; i < n; ++i) v[i] = 0.0;
+        for (int i = j + 1; i < n; ++i) v[i] = a(i, j);
+        v[j + 1] -= alpha;
+        double vv = 0.0;
+        for (int i = j + 1; i < n; ++i) vv += v[i] * v[i];
+        if (vv == 0.0) continue;
+        const double beta = 2.0 / vv;
+        // A <- H A H with H = I - beta v v^T:  p = beta A v, K = beta/2 v^T p, q = p - K v,
+        // A <- A - v q^T - q v^T
+        for (int i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int l = j + 1; l < n; ++l) s += a(i, l) * v[l];
+            p[i] = beta * s;
+        }
+        double K = 0.0;
+        for (int i = j + 1; i < n; ++i) K += v[i] * p[i];
+        K *= 0.5 * beta;
+        for (int i = 0; i < n; ++i) q[i] = p[i] - K * v[i];
+        for (int c = 0; c < n; ++c)
+            for (int r = 0; r < n; ++r) a(r, c) -= v[r] * q[c] + q[r] * v[c];
+        // Q <- Q H
+        for (int r = 0; r < n; ++r) {
+            double s = 0.0;
+            for (int l = j + 1; l < n; ++l) s += Q[(size_t)l * n + r] * v[l];
+            s *= beta;
+            for (int l = j + 1; l < n; ++l) Q[(size_t)l * n + r] -= s * v[l];
+        }
+    }
+    for (int i = 0; i < n; ++i) d[i] = a(i, i);
+    for (int i = 0; i + 1 < n; ++i) e[i] = a(i + 1, i);
+    e[n - 1] = 0.0;
+    // implicit QL on (d, e), rotations applied to the columns of Q
+    const double eps = 2.220446049250313e-16;
+    for (int l = 0; l < n; ++l) {
+        for (int iter = 0; iter < 200; ++iter) {
+            int m = l;
+            for (; m < n - 1; ++m) {
+                const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+                if (std::fabs(e[m]) <= eps * dd) break;
+            }
+            if (m == l) break;
+            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+            double r = std::hypot(g, 1.0);
+            g = d[m] - d[l] + e[l] / (g + (g >= 0 ? r : -r));
+            double s = 1.0, c = 1.0, pp = 0.0;
+            int i = m - 1;
+            bool underflow = false;
+            for (; i >= l; --i) {
+                const double f = s * e[i], b = c * e[i];
+                r = std::hypot(f, g);
+                e[i + 1] = r;
+                if (r == 0.0) {
+                    d[i + 1] -= pp;
+                    e[m] = 0.0;
+                    underflow = true;
+                    break;
+                }
+                s = f / r;
+                c = g / r;
+                g = d[i + 1] - pp;
+                r = (d[i] - g) * s + 2.0 * c * b;
+                pp = s * r;
+                d[i + 1] = g + pp;
+                g = c * r - b;
+                double *qi = &Q[(size_t)i * n], *qi1 = &Q[(size_t)(i + 1) * n];
+                for (int k = 0; k < n; ++k) {
+                    const double t = qi1[k];
+                    qi1[k] = s * qi[k] + c * t;
+                    qi[k] = c * qi[k] - s * t;
+                }
+            }
+            if (underflow) continue;
+            d[l] -= pp;
+            e[l] = g;
+            e[m] = 0.0;
+        }
+    }
+    // sort ascending
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) { return d[x] < d[y]; });
+    w.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        w[i] = d[idx[i]];
+        for (int r = 0; r < n; ++r) A[(size_t)i * n + r] = Q[(size_t)idx[i] * n + r];
+    }
+}
+
+int small_generalized_eig(int m, const double *Ain, const double *Bin, int k, double rank_tol, double *lam, double *C)
+{
+    // scale to unit diagonal, then keep B's numerically nonzero directions
+    std::vector<double> s(m);
+    for (int i = 0; i < m; ++i) {
+        const double b = Bin[(size_t)i * m + i];
+        s[i] = (b > 0 && std::isfinite(b)) ? 1.0 / std::sqrt(b) : 0.0;
+    }
+    std::vector<double> B((size_t)m * m), w;
+    for (int j = 0; j < m; ++j)
+        for (int i = 0; i < m; ++i)
+            B[(size_t)j * m + i] = 0.5 * (Bin[(size_t)j * m + i] + Bin[(size_t)i * m + j]) * s[i] * s[j];
+    sym_eig(m, B, w);
+    const double wmax = w[m - 1];
+    if (!(wmax > 0)) return 0;
+    std::vector<int> keep;
+    for (int i = 0; i < m; ++i)
+        if (w[i] > rank_tol * wmax) keep.push_back(i);
+    const int r = (int)keep.size();
+    // T = S Q_keep Theta^-1/2  (m x r)
+    std::vector<double> T((size_t)m * r);
+    for (int c = 0; c < r; ++c) {
+        const double f = 1.0 / std::sqrt(w[keep[c]]);
+        for (int i = 0; i < m; ++i) T[(size_t)c * m + i] = s[i] * B[(size_t)keep[c] * m + i] * f;
+    }
+    // A' = T^T A T
+    std::vector<double> AT((size_t)m * r), Ap((size_t)r * r);
+    for (int c = 0; c < r; ++c)
+        for (int i = 0; i < m; ++i) {
+            double acc = 0.0;
+            for (int l = 0; l < m; ++l) acc += 0.5 * (Ain[(size_t)l * m + i] + Ain[(size_t)i * m + l]) * T[(size_t)c * m + l];
+            AT[(size_t)c * m + i] = acc;
+        }
+    for (int c = 0; c < r; ++c)
+        for (int i = 0; i < r; ++i) {
+            double acc = 0.0;
+            for (int l = 0; l < m; ++l) acc += T[(size_t)i * m + l] * AT[(size_t)c * m + l];
+            Ap[(size_t)c * r + i] = acc;
+        }
+    for (int c = 0; c < r; ++c)
+        for (int i = 0; i < c; ++i) {
+            const double v = 0.5 * (Ap[(size_t)c * r + i] + Ap[(size_t)i * r + c]);
+            Ap[(size_t)c * r + i] = Ap[(size_t)i * r + c] = v;
+        }
+    std::vector<double> mu;
+    sym_eig(r, Ap, mu);
+    const int kk = std::min(k, r);
+    for (int j = 0; j < kk; ++j) {
+        lam[j] = mu[j];
+        for (int i = 0; i < m; ++i) {
+            double acc = 0.0;
+            for (int l = 0; l < r; ++l) acc += T[(size_t)l * m + i] * Ap[(size_t)j * r + l];
+            C[(size_t)j * m + i] = acc;
+        }
+    }
+    return kk;
+}
+
+// =================================================================== device
+constexpr int kT = 256;
+constexpr int PW = 8;  // panel width
+
+template <typename T>
+__device__ __forceinline__ const T *panel_row(const T *base, int64_t n, int q, int64_t row)
+{
+    return base + ((int64_t)q * n + row) * PW;
+}
+
+// Y = A X for every panel (one warp per (slice, panel), one lane per block
+// row); rows of fixed DOFs are zeroed (the reduce_crs_matrix restriction).
+template <int BS, typename T>
+__global__ void __launch_bounds__(kT) k_spmm(SellView<T> A, int np, const T *__restrict__ X, T *__restrict__ Y,
+                                             const uint8_t *__restrict__ fixed)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t n = A.nb * BS;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = w0; u < A.ns * np; u += nw) {
+        const int64_t s = u / np;
+        const int q = (int)(u - s * np);
+        const int64_t b0 = A.sptr[s];
+        const int wdt = (int)(A.sptr[s + 1] - b0);
+        const int *cp = A.col + b0 * 32 + lane;
+        const T *vp = A.val + b0 * 32 * (BS * BS) + lane;
+        T acc[BS][PW];
+#pragma unroll
+        for (int r = 0; r < BS; ++r)
+#pragma unroll
+            for (int c = 0; c < PW; ++c) acc[r][c] = T(0);
+        for (int k = 0; k < wdt; ++k) {
+            const int col = ld_stream(cp + (int64_t)k * 32);
+            T a[BS * BS];
+#pragma unroll
+            for (int e = 0; e < BS * BS; ++e) a[e] = ld_stream(vp + ((int64_t)k * (BS * BS) + e) * 32);
+#pragma unroll
+            for (int cc = 0; cc < BS; ++cc) {
+                const T *xr = panel_row(X, n, q, (int64_t)BS * col + cc);
+                T xv[PW];
+#pragma unroll
+                for (int c = 0; c < PW; ++c) xv[c] = __ldg(xr + c);
+#pragma unroll
+                for (int r = 0; r < BS; ++r)
+#pragma unroll
+                    for (int c = 0; c < PW; ++c) acc[r][c] = fma(a[r * BS + cc], xv[c], acc[r][c]);
+            }
+        }
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb) {
+#pragma unroll
+            for (int r = 0; r < BS; ++r) {
+                const int64_t i = (int64_t)BS * row + r;
+                const bool f = fixed && fixed[i];
+                T *yr = Y + ((int64_t)q * n + i) * PW;
+#pragma unroll
+                for (int c = 0; c < PW; ++c) yr[c] = f ? T(0) : acc[r][c];
+            }
+        }
+    }
+}
+
+template <typename T>
+struct GramAcc;
+template <>
+struct GramAcc<double> {
+    double v;
+    __device__ void zero() { v = 0.0; }
+    __device__ void add(double a, double b) { v = fma(a, b, v); }
+    __device__ double get() const { return v; }
+};
+template <>
+struct GramAcc<float> {
+    Comp32 v;
+    __device__ void zero() { v = Comp32{0.f, 0.f}; }
+    __device__ void add(float a, float b) { comp_add_prod(v, a, b); }
+    __device__ double get() const { return (double)v.s + (double)v.c; }
+};
+
+constexpr int kGramRows = 16;
+constexpr int kMaxPairsPerThread = 19;  // m <= 96: 96*97/2 = 4656 pairs / 256 threads
+
+// Upper triangles of S^T (K S) and S^T (M S), S = [X W P] (nblk blocks of k
+// columns): each CTA reduces a contiguous row range and writes its partial
+// sums (FP64) to part[cta][2 * npairs].
+template <typename T>
+__global__ void __launch_bounds__(kT)
+    k_gram(int64_t n, int k, int nblk, const T *S0, const T *S1, const T *S2, const T *K0, const T *K1, const T *K2,
+           const T *M0, const T *M1, const T *M2, double *part)
+{
+    extern __shared__ unsigned char smraw[];
+    const int m = nblk * k;
+    const int np = (k + PW - 1) / PW;
+    const int npairs = m * (m + 1) / 2;
+    T *sS = (T *)smraw;
+    T *sK = sS + kGramRows * m;
+    T *sM = sK + kGramRows * m;
+    // this thread's pairs (i <= j)
+    int pi[kMaxPairsPerThread], pj[kMaxPairsPerThread];
+    GramAcc<T> aA[kMaxPairsPerThread], aB[kMaxPairsPerThread];
+    int cnt = 0;
+#pragma unroll
+    for (int u = 0; u < kMaxPairsPerThread; ++u) {
+        // pair p = threadIdx.x + u * blockDim.x -> (i, j), i <= j, row-wise over the upper triangle
+        const int p = threadIdx.x + u * blockDim.x;
+        int i = 0, rem = p < npairs ? p : 0;
+        while (rem >= m - i) {
+            rem -= m - i;
+            ++i;
+        }
+        pi[u] = i;
+        pj[u] = i + rem;
+        aA[u].zero();
+        aB[u].zero();
+        if (p < npairs) cnt = u + 1;
+    }
+    const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
+    const T *SS[3] = {S0, S1, S2}, *KK[3] = {K0, K1, K2}, *MM[3] = {M0, M1, M2};
+    for (int64_t t0 = r0; t0 < r1; t0 += kGramRows) {
+        const int rows = (int)((r1 - t0) < (int64_t)kGramRows ? (r1 - t0) : (int64_t)kGramRows);
+        __syncthreads();
+        // stage rows: element (r, b, q, c) of each block's panel q
+        const int per_row = nblk * np * PW;
+        for (int e = threadIdx.x; e < rows * per_row; e += blockDim.x) {
+            const int r = e / per_row;
+            int rem = e - r * per_row;
+            const int b = rem / (np * PW);
+            rem -= b * np * PW;
+            const int q = rem / PW, c = rem - q * PW;
+            const int col = q * PW + c;
+            if (col >= k) continue;
+            const int64_t off = ((int64_t)q * n + t0 + r) * PW + c;
+            const int j = b * k + col;
+            sS[r * m + j] = SS[b][off];
+            sK[r * m + j] = KK[b][off];
+            sM[r * m + j] = MM[b][off];
+        }
+        __syncthreads();
+        for (int r = 0; r < rows; ++r) {
+            const T *s = sS + r * m, *kk = sK + r * m, *mm = sM + r * m;
+            // fully unrolled with a guard: the accumulators stay in registers
+#pragma unroll
+            for (int u = 0; u < kMaxPairsPerThread; ++u) {
+                if (u < cnt) {
+                    const T si = s[pi[u]];
+                    aA[u].add(si, kk[pj[u]]);
+                    aB[u].add(si, mm[pj[u]]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < kMaxPairsPerThread; ++u) {
+        const int p = threadIdx.x + u * blockDim.x;
+        if (p < npairs) {
+            part[(int64_t)blockIdx.x * 2 * npairs + p] = aA[u].get();
+            part[(int64_t)blockIdx.x * 2 * npairs + npairs + p] = aB[u].get();
+        }
+    }
+}
+
+// Sum the per-CTA partials in CTA order (deterministic).
+__global__ void k_reduce_parts(const double *__restrict__ part, int nparts, int len, double *__restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int b = 0; b < nparts; ++b) s += part[(int64_t)b * len + i];
+        out[i] = s;
+    }
+}
+
+// Pn = W C_w + P C_p ; Xn = X C_x + Pn   (C: m x k column-major, FP64)
+template <typename T>
+__global__ void __launch_bounds__(kT)
+    k_lincomb(int64_t n, int k, int nblk, const T *__restrict__ X, const T *__restrict__ W, const T *__restrict__ P,
+              const double *__restrict__ C, T *__restrict__ Xn, T *__restrict__ Pn)
+{
+    extern __shared__ unsigned char smraw[];
+    T *sC = (T *)smraw;
+    const int m = nblk * k;
+    const int np = (k + PW - 1) / PW;
+    for (int i = threadIdx.x; i < m * k; i += blockDim.x) sC[i] = (T)C[i];
+    __syncthreads();
+    const T *B[3] = {X, W, P};
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+        for (int qo = 0; qo < np; ++qo) {
+            T ax[PW], ap[PW];
+#pragma unroll
+            for (int c = 0; c < PW; ++c) ax[c] = ap[c] = T(0);
+            for (int b = 0; b < nblk; ++b) {
+                for (int qi = 0; qi < np; ++qi) {
+                    const T *src = panel_row(B[b], n, qi, row);
+                    T v[PW];
+#pragma unroll
+                    for (int c = 0; c < PW; ++c) v[c] = src[c];
+#pragma unroll
+                    for (int c = 0; c < PW; ++c) {
+                        const int i = qi * PW + c;
+                        if (i >= k) break;
+                        const T *crow = sC + (b * k + i);  // C[(b k + i), j] at crow[j * m]
+#pragma unroll
+                        for (int o = 0; o < PW; ++o) {
+                            const int j = qo * PW + o;
+                            const T cij = j < k ? crow[(int64_t)j * m] : T(0);
+                            if (b == 0)
+                                ax[o] = fma(v[c], cij, ax[o]);
+                            else
+                                ap[o] = fma(v[c], cij, ap[o]);
+                        }
+                    }
+                }
+            }
+            T *xo = Xn + ((int64_t)qo * n + row) * PW;
+            T *po = Pn + ((int64_t)qo * n + row) * PW;
+#pragma unroll
+            for (int o = 0; o < PW; ++o) {
+                po[o] = ap[o];
+                xo[o] = ax[o] + ap[o];
+            }
+        }
+    }
+}
+
+// R = KX - MX diag(lam); per column: |R_j|^2, |MX_j|^2, max|R_j|  -> part[cta][3k]
+template <typename T>
+__global__ void __launch_bounds__(kT)
+    k_residual(int64_t n, int k, const T *__restrict__ KX, const T *__restrict__ MX, const double *__restrict__ lam,
+               T *__restrict__ R, double *part)
+{
+    __shared__ double sred[3 * 32][kT / 32];
+    const int np = (k + PW - 1) / PW;
+    double rr[32], mm[32], mx[32];
+    for (int j = 0; j < 32; ++j) rr[j] = mm[j] = mx[j] = 0.0;
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+        for (int q = 0; q < np; ++q) {
+            const int64_t off = ((int64_t)q * n + row) * PW;
+#pragma unroll
+            for (int c = 0; c < PW; ++c) {
+                const int j = q * PW + c;
+                if (j >= k) {
+                    R[off + c] = T(0);
+                    continue;
+                }
+                const T mxv = MX[off + c];
+                const T r = KX[off + c] - mxv * (T)lam[j];
+                R[off + c] = r;
+                rr[j] += (double)r * (double)r;
+                mm[j] += (double)mxv * (double)mxv;
+                mx[j] = fmax(mx[j], fabs((double)r));
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int j = 0; j < k; ++j) {
+        double a = warp_sum(rr[j]), b = warp_sum(mm[j]), c = mx[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+        if (lane == 0) {
+            sred[3 * j][wid] = a;
+            sred[3 * j + 1][wid] = b;
+            sred[3 * j + 2][wid] = c;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 * k) {
+        const int j = threadIdx.x / 3, t = threadIdx.x % 3;
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) s = t == 2 ? fmax(s, sred[3 * j + t][w]) : s + sred[3 * j + t][w];
+        part[(int64_t)blockIdx.x * 3 * k + threadIdx.x] = s;
+    }
+}
+
+// W = T R: block Jacobi (BS x BS diagonal blocks of K) per node and column;
+// fixed DOFs zeroed.
+template <int BS, typename T>
+__global__ void __launch_bounds__(kT)
+    k_eig_precond(int64_t nb, int k, const double *__restrict__ dinv, int pc, const T *__restrict__ R,
+                  T *__restrict__ W, const uint8_t *__restrict__ fixed)
+{
+    const int np = (k + PW - 1) / PW;
+    const int64_t n = nb * BS;
+    for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nb;
+         node += (int64_t)gridDim.x * blockDim.x) {
+        double D[BS * BS];
+#pragma unroll
+        for (int e = 0; e < BS * BS; ++e)
+            D[e] = pc == PFG_PC_NONE ? (e % (BS + 1) == 0 ? 1.0 : 0.0) : dinv[node * BS * BS + e];
+        for (int q = 0; q < np; ++q) {
+            const T *r0 = panel_row(R, n, q, (int64_t)BS * node);
+            T *w0 = W + ((int64_t)q * n + (int64_t)BS * node) * PW;
+#pragma unroll
+            for (int c = 0; c < PW; ++c) {
+                double rv[BS];
+#pragma unroll
+                for (int i = 0; i < BS; ++i) rv[i] = r0[i * PW + c];
+#pragma unroll
+                for (int i = 0; i < BS; ++i) {
+                    double v = 0.0;
+#pragma unroll
+                    for (int j = 0; j < BS; ++j) v += D[BS * i + j] * rv[j];
+                    w0[i * PW + c] = (fixed && fixed[(int64_t)BS * node + i]) ? T(0) : (T)v;
+                }
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t splitmix(uint64_t x)
+{
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+
+// X = uniform(-1, 1) from (seed, row, column); padding columns and fixed rows 0.
+template <typename T>
+__global__ void k_random(int64_t n, int k, uint64_t seed, T *__restrict__ X, const uint8_t *__restrict__ fixed)
+{
+    const int np = (k + PW - 1) / PW;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * np * PW;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(i % PW);
+        const int64_t row = (i / PW) % n;
+        const int q = (int)(i / (PW * n));
+        const int j = q * PW + c;
+        const uint64_t h = splitmix(seed * 0x100000001b3ull ^ splitmix((uint64_t)row * 131 + (uint64_t)j));
+        const double u = (double)(h >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+        X[i] = (j < k && !(fixed && fixed[row])) ? (T)u : T(0);
+    }
+}
+
+template <typename S, typename D>
+__global__ void k_convert(int64_t len, const S *__restrict__ a, D *__restrict__ b)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = (D)a[i];
+}
+
+// first nev columns of X (panels) -> column-major n x nev (FP64)
+template <typename T>
+__global__ void k_unpanel(int64_t n, int nev, const T *__restrict__ X, double *__restrict__ out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * nev; i += (int64_t)gridDim.x * blockDim.x) {
+        const int j = (int)(i / n);
+        const int64_t row = i - (int64_t)j * n;
+        out[i] = (double)X[((int64_t)(j / PW) * n + row) * PW + (j % PW)];
+    }
+}
+
+// ===================================================================== driver
+namespace {
+
+int g_sms = 0;
+int sms()
+{
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+template <typename T>
+struct Blocks {
+    DevBuf<T> X, W, P, KX, KW, KP, MX, MW, MP, Xn, Pn, KXn, KPn, MXn, MPn, R;
+    void alloc(size_t len)
+    {
+        for (DevBuf<T> *b : {&X, &W, &P, &KX, &KW, &KP, &MX, &MW, &MP, &Xn, &Pn, &KXn, &KPn, &MXn, &MPn, &R})
+            b->resize(len);
+    }
+};
+
+struct Ctx {
+    int64_t n, nb;
+    int bs;
+    int k, kp, np;
+    cudaStream_t st;
+    const uint8_t *fixed;
+    int launches = 0;
+    DevBuf<double> part, gram, C, lam_d, dinv;
+    std::vector<double> hg, hC, hlam;
+    int ngrid;
+};
+
+template <typename T>
+SellView<T> sell_of(const DevMatrix &A)
+{
+    if constexpr (std::is_same<T, double>::value)
+        return A.sell<double>();
+    else
+        return A.sell<float>();
+}
+
+template <typename T>
+void spmm(Ctx &c, const DevMatrix &A, const T *X, T *Y)
+{
+    const SellView<T> v = sell_of<T>(A);
+    int per = 0;
+    if (A.bs == 3)
+        PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm<3, T>, kT, 0));
+    else
+        PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm<1, T>, kT, 0));
+    const int64_t warps = A.ns * c.np;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)std::max(per, 1) * sms()));
+    if (A.bs == 3)
+        k_spmm<3, T><<<g, kT, 0, c.st>>>(v, c.np, X, Y, c.fixed);
+    else
+        k_spmm<1, T><<<g, kT, 0, c.st>>>(v, c.np, X, Y, c.fixed);
+    PFG_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+template <typename T>
+void gram(Ctx &c, int nblk, const Blocks<T> &B, std::vector<double> &GA, std::vector<double> &GB)
+{
+    const int m = nblk * c.k;
+    const int npairs = m * (m + 1) / 2;
+    const size_t smem = (size_t)3 * kGramRows * m * sizeof(T);
+    const int g = c.ngrid;
+    c.part.ensure((size_t)g * 2 * npairs);
+    c.gram.ensure((size_t)2 * npairs);
+    PFG_CUDA(cudaFuncSetAttribute(k_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_gram<T><<<g, kT, smem, c.st>>>(c.n, c.k, nblk, B.X.p, B.W.p, B.P.p, B.KX.p, B.KW.p, B.KP.p, B.MX.p, B.MW.p,
+                                     B.MP.p, c.part.p);
+    k_reduce_parts<<<grid_for(2 * npairs, 256, 64), 256, 0, c.st>>>(c.part.p, g, 2 * npairs, c.gram.p);
+    PFG_CUDA(cudaGetLastError());
+    c.launches += 2;
+    c.hg.resize((size_t)2 * npairs);
+    PFG_CUDA(cudaMemcpyAsync(c.hg.data(), c.gram.p, 2 * npairs * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    PFG_CUDA(cudaStreamSynchronize(c.st));
+    GA.assign((size_t)m * m, 0.0);
+    GB.assign((size_t)m * m, 0.0);
+    int p = 0;
+    for (int i = 0; i < m; ++i)
+        for (int j = i; j < m; ++j, ++p) {
+            GA[(size_t)j * m + i] = GA[(size_t)i * m + j] = c.hg[p];
+            GB[(size_t)j * m + i] = GB[(size_t)i * m + j] = c.hg[npairs + p];
+        }
+}
+
+template <typename T>
+void lincomb(Ctx &c, int nblk, const T *X, const T *W, const T *P, T *Xn, T *Pn)
+{
+    const int m = nblk * c.k;
+    const size_t smem = (size_t)m * c.k * sizeof(T);
+    PFG_CUDA(cudaFuncSetAttribute(k_lincomb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_lincomb<T><<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, X, W, P, c.C.p, Xn, Pn);
+    PFG_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+// Rayleigh-Ritz on nblk blocks: C, lam on the device; returns pairs found.
+template <typename T>
+int rayleigh_ritz(Ctx &c, int nblk, const Blocks<T> &B, double rank_tol)
+{
+    std::vector<double> GA, GB;
+    gram<T>(c, nblk, B, GA, GB);
+    const int m = nblk * c.k;
+    c.hC.assign((size_t)m * c.k, 0.0);
+    c.hlam.assign(c.k, 0.0);
+    const int got = small_generalized_eig(m, GA.data(), GB.data(), c.k, rank_tol, c.hlam.data(), c.hC.data());
+    if (got < c.k) return got;
+    c.C.ensure((size_t)m * c.k);
+    c.lam_d.ensure((size_t)c.k);
+    PFG_CUDA(cudaMemcpyAsync(c.C.p, c.hC.data(), (size_t)m * c.k * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    PFG_CUDA(cudaMemcpyAsync(c.lam_d.p, c.hlam.data(), c.k * sizeof(double), cudaMemcpyHostToDevice, c.st));
+    return got;
+}
+
+template <typename T>
+void apply_rr(Ctx &c, int nblk, Blocks<T> &B)
+{
+    lincomb<T>(c, nblk, B.X.p, B.W.p, B.P.p, B.Xn.p, B.Pn.p);
+    lincomb<T>(c, nblk, B.KX.p, B.KW.p, B.KP.p, B.KXn.p, B.KPn.p);
+    lincomb<T>(c, nblk, B.MX.p, B.MW.p, B.MP.p, B.MXn.p, B.MPn.p);
+    std::swap(B.X, B.Xn);
+    std::swap(B.P, B.Pn);
+    std::swap(B.KX, B.KXn);
+    std::swap(B.KP, B.KPn);
+    std::swap(B.MX, B.MXn);
+    std::swap(B.MP, B.MPn);
+}
+
+struct ResInfo {
+    std::vector<double> rel, maxabs;
+};
+
+template <typename T>
+ResInfo residuals(Ctx &c, Blocks<T> &B)
+{
+    const int g = std::min(c.ngrid, 1024);
+    c.part.ensure((size_t)g * 3 * c.k);
+    k_residual<T><<<g, kT, 0, c.st>>>(c.n, c.k, B.KX.p, B.MX.p, c.lam_d.p, B.R.p, c.part.p);
+    PFG_CUDA(cudaGetLastError());
+    ++c.launches;
+    std::vector<double> h((size_t)g * 3 * c.k);
+    PFG_CUDA(cudaMemcpyAsync(h.data(), c.part.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c.st));
+    PFG_CUDA(cudaStreamSynchronize(c.st));
+    ResInfo ri;
+    ri.rel.assign(c.k, 0.0);
+    ri.maxabs.assign(c.k, 0.0);
+    for (int j = 0; j < c.k; ++j) {
+        double rr = 0, mm = 0, mx = 0;
+        for (int b = 0; b < g; ++b) {
+            rr += h[(size_t)b * 3 * c.k + 3 * j];
+            mm += h[(size_t)b * 3 * c.k + 3 * j + 1];
+            mx = std::max(mx, h[(size_t)b * 3 * c.k + 3 * j + 2]);
+        }
+        const double den = std::fabs(c.hlam[j]) * std::sqrt(mm);
+        ri.rel[j] = den > 0 ? std::sqrt(rr) / den : std::sqrt(rr);
+        ri.maxabs[j] = mx;
+    }
+    return ri;
+}
+
+// One precision phase.  start: 0 random, 1 X already holds a start block.
+template <typename T>
+int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg, bool fp32_phase, int start,
+          int &iters_left, int &iters_done, double &max_rel, double &ref_r1)
+{
+    const size_t len = (size_t)c.n * c.kp;
+    if (start == 0) {
+        k_random<T><<<grid_for((int64_t)len, 256, sms() * 8), 256, 0, c.st>>>(c.n, c.k, cfg.seed, B.X.p, c.fixed);
+        PFG_CUDA(cudaGetLastError());
+        ++c.launches;
+    }
+    const double rank_tol = fp32_phase ? 1e-9 : 1e-13;
+    spmm<T>(c, K, B.X.p, B.KX.p);
+    spmm<T>(c, M, B.X.p, B.MX.p);
+    // Rayleigh-Ritz on X alone (X of LOBPCG_CRS, SparseClass.f90:2063-2067)
+    if (rayleigh_ritz<T>(c, 1, B, rank_tol) < c.k) throw Error(PFG_E_BREAKDOWN, "LOBPCG: start block is rank deficient");
+    apply_rr<T>(c, 1, B);
+    bool haveP = false;
+    double best = 1e300;
+    int since_best = 0;
+    for (;;) {
+        ResInfo ri = residuals<T>(c, B);
+        max_rel = 0.0;
+        double maxabs = 0.0;
+        for (int j = 0; j < cfg.nev; ++j) {
+            max_rel = std::max(max_rel, ri.rel[j]);
+            maxabs = std::max(maxabs, ri.maxabs[j]);
+        }
+        if (ref_r1 < 0) ref_r1 = maxabs;
+        if (cfg.debug)
+            fprintf(stderr, "[pfg] LOBPCG %s it %d max rel residual %.3e lambda_1 %.9e\n", fp32_phase ? "fp32" : "fp64",
+                    iters_done, max_rel, c.hlam[0]);
+        const bool conv = cfg.stop_rule == 0 ? (maxabs / (ref_r1 > 0 ? ref_r1 : 1.0) < cfg.tol) : (max_rel < cfg.tol);
+        if (conv) return 1;
+        if (fp32_phase) {
+            if (max_rel < cfg.tol_fp32) return 0;
+            if (max_rel < 0.9 * best) {
+                best = max_rel;
+                since_best = 0;
+            } else if (++since_best > 30) {
+                return 0;  // FP32 floor reached
+            }
+        }
+        if (iters_left <= 0) return -1;
+        --iters_left;
+        ++iters_done;
+        // W = T R, its images
+        if (c.bs == 3)
+            k_eig_precond<3, T><<<grid_for(c.nb, kT, sms() * 8), kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond,
+                                                                                B.R.p, B.W.p, c.fixed);
+        else
+            k_eig_precond<1, T><<<grid_for(c.nb, kT, sms() * 8), kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond,
+                                                                                B.R.p, B.W.p, c.fixed);
+        PFG_CUDA(cudaGetLastError());
+        ++c.launches;
+        spmm<T>(c, K, B.W.p, B.KW.p);
+        spmm<T>(c, M, B.W.p, B.MW.p);
+        int nblk = haveP ? 3 : 2;
+        int got = rayleigh_ritz<T>(c, nblk, B, rank_tol);
+        if (got < c.k && nblk == 3) {
+            nblk = 2;  // P became dependent: drop it this iteration
+            got = rayleigh_ritz<T>(c, nblk, B, rank_tol);
+        }
+        if (got < c.k) throw Error(PFG_E_BREAKDOWN, "LOBPCG: Rayleigh-Ritz basis lost rank");
+        apply_rr<T>(c, nblk, B);
+        haveP = true;
+    }
+}
+
+}  // namespace
+
+// Block Jacobi (3x3 node blocks) inverse of K, FP64, for the LOBPCG preconditioner.
+void block_jacobi_inverse(const DevMatrix &A, int pc, double *d64, cudaStream_t st);
+
+EigResult lobpcg_solve(DevMatrix &K, DevMatrix &M, const uint8_t *fixed, const EigConfig &cfg_in, double *lambda,
+                       double *Xout, cudaStream_t st)
+{
+    EigConfig cfg = cfg_in;
+    PFG_CHECK(K.bs == M.bs && K.nb == M.nb, PFG_E_ARG, "eig: A and B must have the same size and block structure");
+    if (cfg.block < cfg.nev) cfg.block = cfg.nev;
+    PFG_CHECK(cfg.nev >= 1 && cfg.block <= 32, PFG_E_ARG, "eig: need 1 <= num_eigen <= block size <= 32");
+    Ctx c;
+    c.n = K.ndof();
+    c.nb = K.nb;
+    c.bs = K.bs;
+    c.k = cfg.block;
+    c.kp = (c.k + PW - 1) / PW * PW;
+    c.np = c.kp / PW;
+    c.st = st;
+    c.fixed = fixed;
+    c.ngrid = sms() * 2;
+    PFG_CHECK(c.n >= 3 * c.k, PFG_E_ARG, "eig: block size too large for the system");
+    EigResult res;
+    cudaEvent_t e0, e1;
+    PFG_CUDA(cudaEventCreate(&e0));
+    PFG_CUDA(cudaEventCreate(&e1));
+    PFG_CUDA(cudaEventRecord(e0, st));
+    c.dinv.ensure((size_t)c.nb * c.bs * c.bs);
+    block_jacobi_inverse(K, cfg.precond == PFG_PC_NONE ? PFG_PC_BLOCK_JACOBI : cfg.precond, c.dinv.p, st);
+    ++c.launches;
+    const size_t len = (size_t)c.n * c.kp;
+    int iters_left = cfg.max_itr, iters_done = 0, rc = -1;
+    double max_rel = 0.0, ref_r1 = -1.0;
+    Blocks<double> B64;
+    B64.alloc(len);
+    build_sell(K, true, cfg.precision == PFG_PREC_MIXED, st);
+    build_sell(M, true, cfg.precision == PFG_PREC_MIXED, st);
+    int start = 0;
+    if (cfg.precision == PFG_PREC_MIXED) {
+        Blocks<float> B32;
+        B32.alloc(len);
+        double r1 = -1.0;
+        rc = phase<float>(c, K, M, B32, cfg, true, 0, iters_left, iters_done, max_rel, r1);
+        res.iterations_fp32 = iters_done;
+        k_convert<float, double><<<grid_for((int64_t)len, 256, sms() * 8), 256, 0, st>>>((int64_t)len, B32.X.p, B64.X.p);
+        PFG_CUDA(cudaGetLastError());
+        ++c.launches;
+        start = 1;
+    }
+    rc = phase<double>(c, K, M, B64, cfg, false, start, iters_left, iters_done, max_rel, ref_r1);
+    res.iterations = iters_done;
+    res.max_rel_residual = max_rel;
+    res.status = rc == 1 ? PFG_OK : PFG_W_NOT_CONVERGED;
+    for (int j = 0; j < cfg.nev; ++j) lambda[j] = c.hlam[j];
+    if (Xout) {
+        k_unpanel<double><<<grid_for(c.n * cfg.nev, 256, sms() * 8), 256, 0, st>>>(c.n, cfg.nev, B64.X.p, Xout);
+        PFG_CUDA(cudaGetLastError());
+        ++c.launches;
+    }
+    PFG_CUDA(cudaEventRecord(e1, st));
+    PFG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    res.ms = ms;
+    res.launches = c.launches;
+    return res;
+}
+
+}  // namespace pfg

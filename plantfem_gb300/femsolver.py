@@ -213,6 +213,46 @@ class FEMSolver:
         self.last_info = info.as_dict()
         return x
 
+    # ------------------------------------------------------------ eigenproblem
+    def keepThisMatrixAs(self, As: str):
+        """FEMSolver_%keepThisMatrixAs (FEMSolverClass.f90:1544-1604)."""
+        N.check(self._lib.pfg_keep_this_matrix_as(self._h, As.encode()))
+
+    def fix_eig(self, IDs):
+        """FEMSolver_%fix_eig (FEMSolverClass.f90:1607-1628)."""
+        ids = _i32(IDs)
+        N.check(self._lib.pfg_fix_eig(self._h, ids.shape[0], N.ptr(ids)))
+
+    def eig(self, num_eigen: int | None = None, block_size: int = 0, precision: str = "fp64",
+            preconditioning: str | None = "BlockJacobi", stop_rule: str = "residual", seed: int = 1,
+            eigen_vectors: bool = True):
+        """(eigen_value, eigen_vectors) = FEMSolver_%eig (FEMSolverClass.f90:1384-1541).
+
+        Always LOBPCG (LOBPCG_CRS, SparseClass.f90:2008-2239) on the matrices
+        kept as "A" and "B"; the reference's dense DSPGVD branch is an O(N^2)
+        CPU path.  Uses LOBPCG_NUM_MODE / LOBPCG_TOL / LOBPCG_MAX_ITR.
+        """
+        nev = int(num_eigen or self.LOBPCG_NUM_MODE)
+        o = N.EigOpts()
+        self._lib.pfg_eig_opts_default(C.byref(o))
+        o.block_size = int(block_size)
+        o.max_itr = int(self.LOBPCG_MAX_ITR)
+        o.tol = float(self.LOBPCG_TOL)
+        o.precision = {"fp64": N.PREC_FP64, "FP64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
+        o.precond = {None: N.PC_NONE, "None": N.PC_NONE, "Jacobi": N.PC_JACOBI, "PointJacobi": N.PC_JACOBI,
+                     "BlockJacobi": N.PC_BLOCK_JACOBI}[preconditioning]
+        o.stop_rule = {"reference": N.EIG_STOP_REFERENCE, "residual": N.EIG_STOP_RESIDUAL}[stop_rule]
+        o.seed = int(seed)
+        o.debug = int(bool(self.debug))
+        lam = np.zeros(nev)
+        n = self.ndof()
+        X = np.zeros((nev, n)) if eigen_vectors else None
+        info = N.Info()
+        N.check(self._lib.pfg_eig(self._h, C.byref(o), nev, N.ptr(lam), None if X is None else N.ptr(X),
+                                  C.byref(info)))
+        self.last_info = info.as_dict()
+        return lam, (None if X is None else X.T)
+
     def solve_device(self, b, x, algorithm="CG", preconditioning="BlockJacobi", precision="mixed",
                      stop_rule=None, stream=None, update_mode=0, reliable_delta=None):
         """Solve with the already-eliminated matrix on device tensors b -> x
