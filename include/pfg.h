@@ -218,6 +218,26 @@ int pfg_crs_spmv_real32(const float *val, const int64_t *row_ptr, const int32_t 
 int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const double *val, const double *rhs,
                           double *x, int64_t n, int64_t nnz, const pfg_solve_opts *opts, pfg_info *info);
 
+/* Allocation-free variant of pfg_linear_solver_crs.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory, such as
+ * a host program whose GPU memory is owned by another runtime or a fixed-size
+ * pool, or code that must not call cudaMalloc/cudaFree (which synchronise the
+ * device) while other work is queued.  The caller passes the 1-based CRS
+ * arrays, rhs and x (x0 on entry, solution on exit) in DEVICE memory; this
+ * call allocates nothing -- no cudaMalloc, cudaFree or allocating library
+ * routine.  Its work vectors and reduction scratch live in one static device
+ * array sized for at most 262,144 unknowns (about 10.5 MB, held on every GPU
+ * that loads the library until the process exits); larger n is rejected with
+ * PFG_E_ARG.  FP64 conjugate gradients only, point Jacobi or no
+ * preconditioner (opts NULL: CG + Jacobi, true relative residual 1e-10).
+ * The first call on a device looks up the array's device address, so make it
+ * before any stream capture.  Every call shares the one array (calls are
+ * serialised and each returns after its stream has finished): work from
+ * other callers that overlaps it on the GPU would race.  stream may be NULL. */
+int pfg_linear_solver_crs_noalloc(const int64_t *d_row_ptr, const int32_t *d_col_idx, const double *d_val,
+                                  const double *d_rhs, double *d_x, int64_t n, const pfg_solve_opts *opts,
+                                  pfg_info *info, void *stream);
+
 /* ------------------------------------------------ device-pointer entry points */
 /* For callers that already hold device memory (the PyTorch binding): the same
  * operations over device pointers on a caller stream (cudaStream_t as void*). */

@@ -96,6 +96,8 @@ SIGNATURES = {
     "pfg_fix_eig": (C.c_int, [_P, _i64, _P]),
     "pfg_eig_opts_default": (None, [C.POINTER(EigOpts)]),
     "pfg_eig": (C.c_int, [_P, C.POINTER(EigOpts), _i32, _P, _P, C.POINTER(Info)]),
+    "pfg_linear_solver_crs_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _i64, C.POINTER(SolveOpts), C.POINTER(Info),
+                                                _P]),
 }
 
 _LIB = None
