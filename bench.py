@@ -41,6 +41,10 @@ TOL = 1e-10
 # The CPU arm times a bounded sample of iterations and scales by this count
 # (GB300 measurement: 1593 iterations, final |b-Kx|/|b| = 1.3e-9).
 REF_ITERS_LOGNORMAL100 = 1593
+# DRAM bytes (read + write) of one k_cg_spmv_u<3,float> launch on lognormal100,
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum); None until
+# captured.
+TRAFFIC_CG_SPMV_FP32 = None
 
 
 def peaks():
@@ -296,20 +300,24 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
              ms_f64, clk, setup_s, t0, t_pat, t_asm, out_extra):
     import torch
     from plantfem_gb300 import _native, linear_solver_crs
-    # kernel roofline: the dominant kernel of the mixed solve is the FP32 block
-    # SpMV with the fused direction update (k_cg_spmv<3,float>)
+    # kernel roofline: the dominant kernel of the mixed solve (streaming update
+    # passes, the default) is the FP32 3x3-block SELL SpMV with the p.q
+    # reduction, k_cg_spmv_u<3,float>; each is timed with CUDA events on the
+    # handle's stream over 20 back-to-back launches
+    import ctypes as C
     prof = {}
-    for kid, name in ((0, "spmv_fp64"), (1, "spmv_fp32"), (2, "cg_spmv_fp32_fused")):
-        import ctypes as C
+    for kid, name in ((0, "spmv_fp64"), (1, "spmv_fp32"), (2, "cg_spmv_fp32_fused"), (5, "cg_spmv_fp32"),
+                      (6, "cg_spmv_fp64")):
         ms, by = C.c_double(), C.c_double()
         _native.check(_native.load().pfg_profile_kernel(s.handle, kid, 20, C.byref(ms), C.byref(by)))
         prof[name] = {"ms": ms.value, "bytes": by.value, "GBs": by.value / (ms.value * 1e-3) / 1e9}
     pk = peaks()
     peak = pk["hbm_gbs"] if pk else 6800.0
-    dom_k = prof["cg_spmv_fp32_fused"]
-    roofline = {"kernel": "k_cg_spmv<3,float> (FP32 3x3-block SpMV + fused p update + p.q)", "bound": "hbm",
+    dom_k = prof["cg_spmv_fp32"]
+    roofline = {"kernel": "k_cg_spmv_u<3,float> (FP32 3x3-block SELL SpMV + p.q)", "bound": "hbm",
                 "achieved": round(dom_k["GBs"], 1), "peak": peak, "unit": "GB/s",
-                "frac": round(dom_k["GBs"] / peak, 4), "traffic": None,
+                "frac": round(dom_k["GBs"] / peak, 4), "traffic": TRAFFIC_CG_SPMV_FP32,
+                "bytes_per_launch": dom_k["bytes"], "ms_per_launch": round(dom_k["ms"], 5),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk else "fallback 6800 GB/s"}
 
     _progress("kernel profiles done")

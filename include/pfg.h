@@ -40,6 +40,7 @@ extern "C" {
 #define PFG_E_INTERNAL (-8)
 #define PFG_E_UNSUPPORTED (-9)
 #define PFG_E_NONFINITE (-10)   /* NaN/Inf in the input or in a Krylov scalar */
+#define PFG_E_ABORTED (-11)     /* a batched solve saw its abort flag set */
 
 /* ----------------------------------------------------------- solve options */
 #define PFG_ALG_BICGSTAB 0      /* bicgstab_CRS_2, FEMSolverClass.f90:2199-2298 (reference default) */
@@ -79,6 +80,9 @@ typedef struct pfg_info {
     double rel_residual;     /* |b - A x| / |b| recomputed in FP64 at exit */
     double iter_residual;    /* recursive residual the stop rule saw */
     double solve_ms;         /* device time of the solve */
+    int32_t fallback;        /* mixed: 1 when the FP32 inner iterations failed (breakdown,
+                                overflow, or FP64 residuals that stopped falling) and the
+                                solve finished in FP64 from the current x */
 } pfg_info;
 
 /* Fill opts with the reference's defaults (BiCGSTAB, FP64, no preconditioner,
@@ -157,6 +161,19 @@ int pfg_zeros(pfg_solver *h);
  * mark 1-based DOF ids fixed; values NULL -> every id gets `value`.  Ids < 1 or
  * beyond the system size are skipped, as the reference's first call does. */
 int pfg_fix(pfg_solver *h, int64_t n, const int32_t *ids, const double *values, double value);
+
+/* The Dirichlet elimination that FEMSolver_%solve performs before its Krylov
+ * solve (FEMSolverClass.f90:1707-1756), on its own: afterwards the stored
+ * matrix and RHS are the eliminated system (pfg_dev_solve solves it). */
+int pfg_eliminate(pfg_solver *h);
+
+/* getElementCauchyStress(displacement, E, v, option) (FEMDomainClass.f90:15249-15330,
+ * StressMatrix :11912-12035): cell-averaged Cauchy stress of every element from the
+ * node-interleaved displacement (3*nn, host).  option 0: full 3x3 tensors (out: ne*9,
+ * row-major), 1: I1 = trace ("I1"), 2: mean stress trace/3 ("p") (out: ne).  E, v:
+ * n_prop = 1 or ne values. */
+int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop, const double *E, const double *v,
+                       int32_t option, double *out);
 
 /* x = FEMSolver_%solve() (FEMSolverClass.f90:1697-1825): Dirichlet elimination
  * (mutates the stored matrix and RHS in place, as the reference), Krylov solve,
@@ -247,13 +264,95 @@ int pfg_dev_spmv(pfg_solver *h, const double *d_x, double *d_y, void *stream);
 int pfg_dev_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *d_b, double *d_x, pfg_info *info,
                   void *stream);
 
+/* Device-array forms used by the PyTorch binding (stream NULL: the handle's own
+ * stream, after the caller's work on the legacy default stream). */
+/* StiffnessMatrix loop with device E / v (n_prop = 1 or ne values); adds into K. */
+int pfg_dev_assemble_stiffness(pfg_solver *h, int64_t n_prop, const double *d_E, const double *d_nu, void *stream);
+/* setRHS from device memory. */
+int pfg_dev_set_rhs(pfg_solver *h, int64_t n, const double *d_rhs, void *stream);
+/* Adjoint sensitivity of a per-element Young's modulus (no reference counterpart:
+ * the reference has no adjoint).  For K(E) u = f and an adjoint solution lambda
+ * of K lambda = dL/du (zero at fixed DOFs), writes dL/dE_e = -lambda_e^T
+ * (dK_e/dE_e) u_e for every element, with dK_e/dE_e the element stiffness at
+ * E = 1 (StiffnessMatrixFEMDomain is linear in E).  u, lambda: 3*nn device arrays. */
+int pfg_dev_adjoint_grad_E(pfg_solver *h, const double *d_u, const double *d_lambda, int64_t n_prop,
+                           const double *d_nu, double *d_grad, void *stream);
+
+/* ------------------------------------------------------------ batched solves */
+/* No single reference call: plantFEM solves one organ mesh per FEMSolver_
+ * object and calls FEMSolver_%solve on each in turn (FEMSolverClass.f90:1707
+ * onwards, one mesh at a time).  A batch takes many such handles -- each set
+ * up exactly as for pfg_solve: setCRS, assembly, fix -- and solves all of them
+ * in ONE persistent kernel launch (replayed from a CUDA graph): each system is
+ * solved by one CTA, or by a thread-block cluster for the largest ones, taking
+ * jobs from an atomic queue in order of decreasing estimated cost.  Handles
+ * must hold 3-DOF (3x3-block) systems on the batch's device, must outlive the
+ * batch's use of them and must not be used while a batched solve runs; re-bind
+ * (pfg_batch_set) after changing any of them. */
+typedef struct pfg_batch pfg_batch;
+
+typedef struct pfg_batch_config {
+    int32_t threads;       /* threads per CTA (256, 512 or 1024): block rows of one CTA tile */
+    int32_t cluster;       /* CTAs that solve one large system together (1, 2, 4 or 8) */
+    double team_fraction;  /* share of the systems, largest estimated cost first, solved by a
+                              whole cluster; the rest are solved by single CTAs */
+} pfg_batch_config;
+
+typedef struct pfg_batch_info {
+    pfg_batch_config config;   /* configuration used */
+    int32_t launches;          /* kernel launches of the solve (the persistent kernel: 1) */
+    int32_t max_iterations;    /* largest CG iteration count of any system */
+    int64_t total_iterations;  /* sum over the systems */
+    double max_rel_residual;   /* largest true |b - Kx| / |b| */
+    double solve_ms;           /* device time of the launch (CUDA events) */
+    int32_t fallbacks;         /* mixed: systems solved in FP64 (pfg_info.fallback != 0) */
+} pfg_batch_info;
+
+int pfg_batch_create(pfg_batch **out);
+int pfg_batch_destroy(pfg_batch *b);
+/* Bind `count` handles: applies each handle's Dirichlet elimination as
+ * pfg_solve does, builds the sliced matrix copies, pools the work vectors. */
+int pfg_batch_set(pfg_batch *b, int64_t count, pfg_solver *const *handles);
+/* Solve every bound system from x0 = 0 to the true relative residual
+ * opts->relative_er.  opts->algorithm must be PFG_ALG_CG (the systems are
+ * symmetric positive definite; others: PFG_E_UNSUPPORTED); precision FP64 or
+ * MIXED (FP32 CG with compensated dots and FP64 residual replacement);
+ * precond NONE, JACOBI or BLOCK_JACOBI; itrmax per system.  opts NULL: mixed,
+ * block Jacobi, 1e-10.  x_out NULL, or `count` host arrays (3 nn each) that
+ * receive the solutions with the fixed values restored; infos NULL or `count`
+ * records.  A mixed solve keeps an FP32 correction only when it lowers the
+ * FP64 residual and hands a system over to FP64 CG when FP32 fails on it
+ * (infos[m].fallback = 1); the batch remembers those systems, and the ones
+ * whose FP32 iterations exceed 1.5x their FP64 iterations, and solves them in
+ * FP64 from the next mixed solve on (fallback = 2) until pfg_batch_set.
+ * Returns PFG_OK, the first negative status of any system, or
+ * PFG_W_NOT_CONVERGED. */
+int pfg_batch_solve(pfg_batch *b, const pfg_solve_opts *opts, double *const *x_out, pfg_info *infos,
+                    pfg_batch_info *binfo);
+/* Solution of system `index` of the last batched solve. */
+int pfg_batch_get_x(pfg_batch *b, int64_t index, double *x_out);
+/* Launch configuration by hand (checked), and the one in use. */
+int pfg_batch_set_config(pfg_batch *b, const pfg_batch_config *cfg);
+int pfg_batch_get_config(pfg_batch *b, pfg_batch_config *cfg, int32_t *tuned);
+/* Autotuner: times full batched solves of the bound systems with `opts` over
+ * candidate configurations (cluster size, then threads per CTA, then team
+ * share), keeps the fastest for later solves and returns it. */
+int pfg_batch_tune(pfg_batch *b, const pfg_solve_opts *opts, pfg_batch_config *best, double *best_ms);
+/* Host address of the batch's abort flag (host-mapped memory, 0 at creation).
+ * Setting it to 1 from any host thread makes every team retire its system with
+ * PFG_E_ABORTED at its next check (every 64 iterations); the caller resets it. */
+int pfg_batch_abort_flag(pfg_batch *b, volatile int32_t **flag);
+
 /* ------------------------------------------------------------ instrumentation */
 /* No counterpart in the reference (it has only wall-clock timers, TimeClass.f90).
  * Times `reps` back-to-back launches of one kernel on the handle's matrix with
  * CUDA events on the handle's stream and returns the mean milliseconds per
  * launch and the algorithmic bytes one launch moves.  kernel: 0 = FP64 block
  * SpMV, 1 = FP32 block SpMV, 2 = the FP32 CG SpMV with the fused direction
- * update (the dominant kernel of the mixed-precision solve). */
+ * update, 3 / 4 = FP64 / FP32 warp-per-row BCRS SpMV, 5 / 6 = the FP32 / FP64
+ * CG SpMV with the p.q reduction (the dominant kernels of the mixed and FP64
+ * solves with streaming update passes, the default).  Kernels 2, 5 and 6 need
+ * a symmetric positive definite (eliminated) matrix. */
 int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, double *ms_per_launch, double *bytes_per_launch);
 
 #ifdef __cplusplus

@@ -17,6 +17,7 @@ PFG_W_NOT_CONVERGED = 1
 ERRORS = {
     -1: "PFG_E_ARG", -2: "PFG_E_STATE", -3: "PFG_E_MISSING_SLOT", -4: "PFG_E_BREAKDOWN", -5: "PFG_E_NOMEM",
     -6: "PFG_E_CUDA", -7: "PFG_E_DETJ", -8: "PFG_E_INTERNAL", -9: "PFG_E_UNSUPPORTED", -10: "PFG_E_NONFINITE",
+    -11: "PFG_E_ABORTED",
 }
 
 ALG_BICGSTAB, ALG_CG = 0, 1
@@ -47,15 +48,33 @@ class EigOpts(C.Structure):
 EIG_STOP_REFERENCE, EIG_STOP_RESIDUAL = 0, 1
 
 
+class BatchConfig(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("cluster", C.c_int32), ("team_fraction", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {"threads": self.threads, "cluster": self.cluster, "team_fraction": self.team_fraction}
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("config", BatchConfig), ("launches", C.c_int32), ("max_iterations", C.c_int32),
+                ("total_iterations", C.c_int64), ("max_rel_residual", C.c_double), ("solve_ms", C.c_double),
+                ("fallbacks", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {"config": self.config.as_dict(), "launches": self.launches, "max_iterations": self.max_iterations,
+                "total_iterations": self.total_iterations, "max_rel_residual": self.max_rel_residual,
+                "solve_ms": self.solve_ms, "fallbacks": self.fallbacks}
+
+
 class Info(C.Structure):
     _fields_ = [("status", C.c_int32), ("iterations", C.c_int32), ("replacements", C.c_int32),
                 ("kernel_launches", C.c_int32), ("rel_residual", C.c_double), ("iter_residual", C.c_double),
-                ("solve_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("fallback", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {"status": self.status, "iterations": self.iterations, "replacements": self.replacements,
                 "kernel_launches": self.kernel_launches, "rel_residual": self.rel_residual,
-                "iter_residual": self.iter_residual, "solve_ms": self.solve_ms}
+                "iter_residual": self.iter_residual, "solve_ms": self.solve_ms, "fallback": self.fallback}
 
 
 _P = C.c_void_p
@@ -98,6 +117,20 @@ SIGNATURES = {
     "pfg_eig": (C.c_int, [_P, C.POINTER(EigOpts), _i32, _P, _P, C.POINTER(Info)]),
     "pfg_linear_solver_crs_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _i64, C.POINTER(SolveOpts), C.POINTER(Info),
                                                 _P]),
+    "pfg_eliminate": (C.c_int, [_P]),
+    "pfg_element_stress": (C.c_int, [_P, _P, _i64, _P, _P, _i32, _P]),
+    "pfg_dev_assemble_stiffness": (C.c_int, [_P, _i64, _P, _P, _P]),
+    "pfg_dev_set_rhs": (C.c_int, [_P, _i64, _P, _P]),
+    "pfg_dev_adjoint_grad_E": (C.c_int, [_P, _P, _P, _i64, _P, _P, _P]),
+    "pfg_batch_create": (C.c_int, [C.POINTER(_P)]),
+    "pfg_batch_destroy": (C.c_int, [_P]),
+    "pfg_batch_set": (C.c_int, [_P, _i64, _P]),
+    "pfg_batch_solve": (C.c_int, [_P, C.POINTER(SolveOpts), _P, _P, C.POINTER(BatchInfo)]),
+    "pfg_batch_get_x": (C.c_int, [_P, _i64, _P]),
+    "pfg_batch_set_config": (C.c_int, [_P, C.POINTER(BatchConfig)]),
+    "pfg_batch_get_config": (C.c_int, [_P, C.POINTER(BatchConfig), C.POINTER(_i32)]),
+    "pfg_batch_tune": (C.c_int, [_P, C.POINTER(SolveOpts), C.POINTER(BatchConfig), C.POINTER(_d)]),
+    "pfg_batch_abort_flag": (C.c_int, [_P, C.POINTER(C.POINTER(_i32))]),
 }
 
 _LIB = None

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "assembly.cuh"
+#include "batch.cuh"
 
 namespace pfg {
 
@@ -140,6 +141,7 @@ void fill_info(pfg_info *info, const SolveResult &r, int precision)
     info->rel_residual = r.rel_residual;
     info->iter_residual = r.iter_residual;
     info->solve_ms = r.ms;
+    info->fallback = r.fallback;
 }
 
 int solve_status(const SolveResult &r)
@@ -757,6 +759,7 @@ int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *
             info->rel_residual = r.max_rel_residual;
             info->iter_residual = r.max_rel_residual;
             info->solve_ms = r.ms;
+            info->fallback = 0;
         }
     });
     if (rc != PFG_OK) return rc;
@@ -765,3 +768,135 @@ int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- elimination, stress, adjoint
+namespace {
+
+cudaStream_t pick_stream(pfg_solver *h, void *stream)
+{
+    if (stream) {
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        return (cudaStream_t)stream;
+    }
+    PFG_CUDA(cudaStreamSynchronize((cudaStream_t)0));  // order after the caller's default-stream work
+    return h->st;
+}
+
+void check_prop_device(pfg_solver *h, int64_t n_prop)
+{
+    need(n_prop == 1 || n_prop == h->mesh.ne, PFG_E_ARG, "property arrays need 1 or number_of_element values");
+}
+
+}  // namespace
+
+extern "C" {
+
+int pfg_eliminate(pfg_solver *h)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "eliminate before setCRS");
+        flush_pending(h);
+        apply_fix_device(h);
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop, const double *E, const double *v,
+                       int32_t option, double *out)
+{
+    return guard([&] {
+        need(h && displacement && E && v && out, PFG_E_ARG, "NULL argument");
+        need(option >= 0 && option <= 2, PFG_E_ARG, "option: 0 tensor, 1 I1, 2 mean stress");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "stress before setDomain");
+        const int64_t ne = h->mesh.ne, n = 3 * h->mesh.nn;
+        DevBuf<double> du((size_t)n), dE, dnu, S((size_t)ne * 9);
+        upload_prop(h, n_prop, E, dE, "E");
+        upload_prop(h, n_prop, v, dnu, "v");
+        PFG_CUDA(cudaMemcpyAsync(du.p, displacement, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        element_stress(h->mesh, du.p, dE.p, dnu.p, n_prop == 1, S.p, h->st);
+        std::vector<double> hs((size_t)ne * 9);
+        PFG_CUDA(cudaMemcpyAsync(hs.data(), S.p, ne * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        if (option == 0) {
+            memcpy(out, hs.data(), ne * 9 * sizeof(double));
+        } else {
+            for (int64_t e = 0; e < ne; ++e) {
+                const double tr = hs[e * 9] + hs[e * 9 + 4] + hs[e * 9 + 8];
+                out[e] = option == 1 ? tr : tr / 3.0;  // getElementCauchyStress options (FEMDomainClass.f90:15310-15314)
+            }
+        }
+    });
+}
+
+int pfg_dev_assemble_stiffness(pfg_solver *h, int64_t n_prop, const double *d_E, const double *d_nu, void *stream)
+{
+    return guard([&] {
+        need(h && d_E && d_nu, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "assemble before setDomain");
+        ensure_crs(h);
+        flush_pending(h);
+        check_prop_device(h, n_prop);
+        cudaStream_t st = pick_stream(h, stream);
+        assemble_elements(h->mesh, h->K, 0, d_E, d_nu, n_prop == 1, st);
+    });
+}
+
+int pfg_dev_set_rhs(pfg_solver *h, int64_t n, const double *d_rhs, void *stream)
+{
+    return guard([&] {
+        need(h && d_rhs, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        ensure_crs(h);
+        need(n == h->ndof(), PFG_E_ARG, "setRHS: size differs from the CRS matrix");
+        cudaStream_t st = pick_stream(h, stream);
+        PFG_CUDA(cudaMemcpyAsync(h->rhs.p, d_rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        PFG_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int pfg_dev_adjoint_grad_E(pfg_solver *h, const double *d_u, const double *d_lambda, int64_t n_prop,
+                           const double *d_nu, double *d_grad, void *stream)
+{
+    return guard([&] {
+        need(h && d_u && d_lambda && d_nu && d_grad, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_mesh, PFG_E_STATE, "adjoint before setDomain");
+        check_prop_device(h, n_prop);
+        cudaStream_t st = pick_stream(h, stream);
+        adjoint_grad_E(h->mesh, d_u, d_lambda, d_nu, n_prop == 1, d_grad, st);
+    });
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------- batched solves
+namespace pfg {
+
+// Prepares handle h for a batched solve: flushes buffered element matrices,
+// applies the Dirichlet elimination FEMSolver_%solve applies before solving
+// (FEMSolverClass.f90:1707-1756), refreshes the sliced FP64 and FP32 copies
+// and describes what the batched kernel reads.
+BatchSource batch_bind(pfg_solver *h)
+{
+    PFG_CHECK(h != nullptr, PFG_E_ARG, "NULL handle in a batch");
+    std::lock_guard<std::mutex> lk(h->mu);
+    PFG_CHECK(h->have_crs, PFG_E_STATE, "batch member without a CRS matrix");
+    PFG_CHECK(h->K.bs == 3, PFG_E_UNSUPPORTED, "batched solves take 3-DOF (3x3-block) systems");
+    flush_pending(h);
+    apply_fix_device(h);
+    build_sell(h->K, true, true, h->st);
+    PFG_CUDA(cudaStreamSynchronize(h->st));
+    BatchSource s;
+    s.K = &h->K;
+    s.b = h->rhs.p;
+    s.fixed = h->have_fix ? h->fixed_d.p : nullptr;
+    s.fixval = h->have_fix ? h->fixval_d.p : nullptr;
+    s.device = h->device;
+    return s;
+}
+
+}  // namespace pfg

@@ -450,7 +450,13 @@ __global__ void __launch_bounds__(kThreads)
             const float rn = sqrtf((float)rr);
             S->rr32 = (float)rr;
             S->rmax32 = fmaxf(S->rmax32, rn);
-            if ((double)rn < delta * (double)S->rmax32 || (double)rn <= tol * sqrt(S->bb)) {
+            S->rmin32 = fminf(S->rmin32, rn);
+            // replace on progress (delta), at the tolerance, or when the FP32
+            // recursion diverges (1000x above its minimum since the last
+            // replacement); the host keeps the correction only if it lowers
+            // the FP64 residual
+            if ((double)rn < delta * (double)S->rmax32 || (double)rn <= tol * sqrt(S->bb) ||
+                rn > 1000.f * S->rmin32) {
                 S->need_update = 1;  // replacement recomputes rho and beta
             } else {
                 S->beta32 = (float)(rho_n / (double)S->rho32);
@@ -497,6 +503,7 @@ __global__ void __launch_bounds__(kThreads)
             S->rho32 = rho_n;
             S->rr32 = tot[1];
             S->rmax32 = sqrtf(tot[1]);
+            S->rmin32 = S->rmax32;
             S->need_update = 0;
         }
     }
@@ -988,6 +995,7 @@ void Krylov::prepare(const DevMatrix &A, const KConfig &cfg, cudaStream_t st)
         pB32_.ensure(nn);
         q32_.ensure(nn);
         x32_.ensure(nn);
+        xb_.ensure(nn);
         if (cfg.algorithm == PFG_ALG_BICGSTAB) {
             r032_.ensure(nn);
             yA32_.ensure(nn);
@@ -1024,18 +1032,24 @@ void block_jacobi_inverse(const DevMatrix &A, int pc, double *d64, cudaStream_t 
     PFG_CUDA(cudaGetLastError());
 }
 
+void block_jacobi(const DevMatrix &A, int precond, double *d64, float *d32, cudaStream_t st)
+{
+    if (precond == PFG_PC_NONE || A.nb == 0) return;
+    const int g = grid_for(A.nb, 256, sm_count() * 8);
+    if (A.bs == 3)
+        k_precond<3><<<g, 256, 0, st>>>(A.view<double>(), precond, d64, d32);
+    else
+        k_precond<1><<<g, 256, 0, st>>>(A.view<double>(), precond, d64, d32);
+    PFG_CUDA(cudaGetLastError());
+}
+
 void Krylov::build_precond(const DevMatrix &A, int precond, bool fp32, cudaStream_t st)
 {
     if (precond == PFG_PC_NONE) return;
     const size_t m = (size_t)std::max<int64_t>(A.nb * A.bs * A.bs, 1);
     dinv_.ensure(m);
     if (fp32) dinv32_.ensure(m);
-    const int g = grid_for(A.nb, 256, sm_count() * 8);
-    if (A.bs == 3)
-        k_precond<3><<<g, 256, 0, st>>>(A.view<double>(), precond, dinv_.p, fp32 ? dinv32_.p : nullptr);
-    else
-        k_precond<1><<<g, 256, 0, st>>>(A.view<double>(), precond, dinv_.p, fp32 ? dinv32_.p : nullptr);
-    PFG_CUDA(cudaGetLastError());
+    block_jacobi(A, precond, dinv_.p, fp32 ? dinv32_.p : nullptr, st);
     ++launches_;
 }
 
@@ -1209,9 +1223,26 @@ SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfi
     PFG_CUDA(cudaEventRecord(e0, st));
     SolveResult res;
     try {
-        if (cfg.precision == PFG_PREC_MIXED)
+        if (cfg.precision == PFG_PREC_MIXED) {
             res = run_mixed(A, b, x, cfg, st);
-        else if (cfg.algorithm == PFG_ALG_CG)
+            if (res.fallback) {
+                // The FP32 copy of the operator failed (repeated breakdowns or
+                // overflow, or FP64 residuals that stopped falling: a system
+                // whose conditioning is beyond FP32).  Finish in FP64 from the
+                // current x, within what is left of itrmax.
+                KConfig c64 = cfg;
+                c64.precision = PFG_PREC_FP64;
+                c64.stop_rule = PFG_STOP_TRUE_RELATIVE;
+                c64.itrmax = std::max(1, cfg.itrmax - res.iterations);
+                prepare(A, c64, st);
+                SolveResult r2 = cfg.algorithm == PFG_ALG_CG ? run_cg64(A, b, x, c64, st)
+                                                             : run_bicgstab64(A, b, x, c64, st);
+                r2.iterations += res.iterations;
+                r2.replacements = res.replacements;
+                r2.fallback = 1;
+                res = r2;
+            }
+        } else if (cfg.algorithm == PFG_ALG_CG)
             res = run_cg64(A, b, x, cfg, st);
         else
             res = run_bicgstab64(A, b, x, cfg, st);
@@ -1359,6 +1390,10 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
     return res;
 }
 
+// Replacements in a row whose FP64 residual did not fall by 10 % before the
+// mixed solve hands over to FP64.
+constexpr int kMixedStall = 4;
+
 SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st)
 {
     SolveResult res;
@@ -1415,41 +1450,79 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
     bool first = true;
     KState h;
     memset(&h, 0, sizeof(h));
+    double best_rel = 0.0, prev_rel = 0.0;
+    int stall = 0, failures = 0;
     for (;;) {
-        // residual replacement: x64 += x32; r64 = b - A64 x64; r32 = r64
+        // residual replacement: x64 += x32; r64 = b - A64 x64; r32 = r64.
+        // The FP32 correction is kept only if it lowers the FP64 residual
+        // (x is backed up before the fold); an overflowed one is dropped.
+        bool rejected = false;
         if (!first) {
             if (h.poisoned) {
-                // the last FP32 update overflowed: keep x64, drop the correction
                 PFG_CUDA(cudaMemsetAsync(x32_.p, 0, n * sizeof(float), st));
                 const int zero = 0;
                 PFG_CUDA(cudaMemcpyAsync(&state_.p->poisoned, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+                rejected = true;
             } else {
+                PFG_CUDA(cudaMemcpyAsync(xb_.p, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
                 k_fold<<<gv, 256, 0, st>>>(n, x, x32_.p);
                 PFG_CUDA(cudaGetLastError());
                 ++launches_;
             }
         }
-        const double rel = true_residual(A, b, x, r_.p, st);
+        double rel = true_residual(A, b, x, r_.p, st);
+        if (!first && !rejected && !(rel < prev_rel)) {
+            PFG_CUDA(cudaMemcpyAsync(x, xb_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            rel = true_residual(A, b, x, r_.p, st);
+            rejected = true;
+        }
+        prev_rel = rel;
+        failures = rejected ? failures + 1 : 0;
+        if (failures >= 2 && rel > cfg.relative_er) {
+            // two FP32 passes in a row made no progress: finish in FP64
+            res.fallback = 1;
+            res.iterations = h.iter;
+            res.replacements = h.replacements;
+            res.rel_residual = rel;
+            return res;
+        }
         res.rel_residual = rel;
+        // FP64 residuals that stopped falling (10 % per replacement) while
+        // above the target: the FP32 operator has reached its accuracy
+        if (first || rel < 0.9 * best_rel) {
+            best_rel = rel;
+            stall = 0;
+        } else if (++stall >= kMixedStall && rel > cfg.relative_er) {
+            res.fallback = 1;
+            res.iterations = h.iter;
+            res.replacements = h.replacements;
+            return res;
+        }
         k_replace<<<gv, 256, 0, st>>>(n, r_.p, r32_.p, state_.p, cfg.relative_er);
         PFG_CUDA(cudaGetLastError());
         launches_ += 2;  // k_replace and the restart below
         if (cg) {
+            // a rejected pass restarts from p = z (its direction may be spoilt)
+            const int keep = (first || rejected) ? 0 : 1;
+            if (rejected) {
+                PFG_CUDA(cudaMemsetAsync(pA32_.p, 0, n * sizeof(float), st));
+                PFG_CUDA(cudaMemsetAsync(pB32_.p, 0, n * sizeof(float), st));
+            }
             if (A.bs == 3)
                 k_cg_restart<3, float><<<g, kThreads, 0, st>>>(A.nb, r32_.p, z32_.p, dinv32_.p, cfg.precond,
                                                                state_.p, partials_.p, partials32_.p, ticket_.p,
-                                                               first ? 0 : 1);
+                                                               keep);
             else
                 k_cg_restart<1, float><<<g, kThreads, 0, st>>>(A.nb, r32_.p, z32_.p, dinv32_.p, cfg.precond,
                                                                state_.p, partials_.p, partials32_.p, ticket_.p,
-                                                               first ? 0 : 1);
+                                                               keep);
         } else {
             // Keep the search direction and the shadow residual r0 while r0.r
             // still carries FP32 digits (|cos(r0, r)| > 1e-3); otherwise, or
             // after a breakdown, restart with r0 = r and p = r.  Keeping the
             // first r0 for good makes r0.r lose every FP32 digit once |r| has
             // dropped by many orders.
-            bool full = first || h.breakdowns > 0;
+            bool full = first || rejected || h.breakdowns > 0;
             if (!full) {
                 k_bicg_restart<float><<<g, kThreads, 0, st>>>(n, r32_.p, r032_.p, state_.p, partials_.p,
                                                               partials32_.p, ticket_.p, 0, 1);
@@ -1472,10 +1545,12 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
         first = false;
         read_state(h, st);
         if (h.breakdowns > 3 && !h.done) {
-            // repeated FP32 breakdowns with no completed iteration in between
-            res.status = PFG_E_BREAKDOWN;
-            h.status = PFG_E_BREAKDOWN;
-            break;
+            // repeated FP32 breakdowns with no completed iteration in between:
+            // x holds the folded solution, the caller finishes in FP64
+            res.fallback = 1;
+            res.iterations = h.iter;
+            res.replacements = h.replacements;
+            return res;
         }
         if (cfg.debug != 0)
             fprintf(stderr, "[pfg] mixed iter %d replacement %d |b-Ax|/|b| %.3e\n", h.iter, h.replacements, rel);
@@ -1516,15 +1591,15 @@ __global__ void k_fill(double *a, int64_t n, double v)
 
 void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
 {
-    PFG_CHECK(kernel >= 0 && kernel <= 4 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel >= 0 && kernel <= 6 && reps > 0, PFG_E_ARG, "bad profile request");
     const int64_t n = A.ndof();
     const double bs2 = (double)(A.bs * A.bs);
     // algorithmic bytes: values and block columns once, row pointers (int64)
     // once, source vector once, result once -- padding slots are overhead
     const double idx = (double)A.nnzb * 4.0 + (double)(A.nb + 1) * 8.0;
-    const bool f64 = kernel == 0 || kernel == 3;
+    const bool f64 = kernel == 0 || kernel == 3 || kernel == 6;
     if (kernel == 4 && !A.v32_valid) make_v32(A, st);
-    if (kernel <= 2) build_sell(A, f64, !f64, st);
+    if (kernel <= 2 || kernel >= 5) build_sell(A, f64, !f64, st);
     const int gv = grid_for(n, 256, sm_count() * 8);
     const int gb = row_grid(A.nb);
     DevBuf<double> x64, y64;
@@ -1541,6 +1616,8 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
     const int g0 = A.bs == 3 ? resident_grid(k_spmv_sell<3, double>, A.ns) : resident_grid(k_spmv_sell<1, double>, A.ns);
     const int g1 = A.bs == 3 ? resident_grid(k_spmv_sell<3, float>, A.ns) : resident_grid(k_spmv_sell<1, float>, A.ns);
     const int g2 = A.bs == 3 ? resident_grid(k_cg_spmv<3, float>, A.ns) : resident_grid(k_cg_spmv<1, float>, A.ns);
+    const int g5 = A.bs == 3 ? resident_grid(k_cg_spmv_u<3, float>, A.ns) : resident_grid(k_cg_spmv_u<1, float>, A.ns);
+    const int g6 = A.bs == 3 ? resident_grid(k_cg_spmv_u<3, double>, A.ns) : resident_grid(k_cg_spmv_u<1, double>, A.ns);
     partials_.ensure((size_t)sm_count() * (2048 / kThreads) * 4 + 8);
     partials32_.ensure((size_t)sm_count() * (2048 / kThreads) * 8 + 16);
     PFG_CUDA(cudaMemcpyAsync(state_.p, &hs, sizeof(KState), cudaMemcpyHostToDevice, st));
@@ -1561,6 +1638,22 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
             else
                 k_cg_spmv<1, float><<<g2, kThreads, 0, st>>>(A.sell<float>(), x32.p, p32.p, y32.p, q32.p, state_.p,
                                                              partials_.p, partials32_.p, ticket_.p);
+            break;
+        case 5:
+            if (A.bs == 3)
+                k_cg_spmv_u<3, float><<<g5, kThreads, 0, st>>>(A.sell<float>(), x32.p, y32.p, state_.p, partials_.p,
+                                                               partials32_.p, ticket_.p);
+            else
+                k_cg_spmv_u<1, float><<<g5, kThreads, 0, st>>>(A.sell<float>(), x32.p, y32.p, state_.p, partials_.p,
+                                                               partials32_.p, ticket_.p);
+            break;
+        case 6:
+            if (A.bs == 3)
+                k_cg_spmv_u<3, double><<<g6, kThreads, 0, st>>>(A.sell<double>(), x64.p, y64.p, state_.p, partials_.p,
+                                                                partials32_.p, ticket_.p);
+            else
+                k_cg_spmv_u<1, double><<<g6, kThreads, 0, st>>>(A.sell<double>(), x64.p, y64.p, state_.p, partials_.p,
+                                                                partials32_.p, ticket_.p);
             break;
         case 3:
             if (A.bs == 3) k_spmv<3, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
@@ -1603,7 +1696,7 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ms = (double)t / reps;
-    if (kernel == 2) {
+    if (kernel == 2 || kernel >= 5) {
         KState h;
         read_state(h, st);
         PFG_CHECK(!h.done, PFG_E_BREAKDOWN, "profiled CG SpMV hit p.Ap <= 0 (matrix not positive definite)");

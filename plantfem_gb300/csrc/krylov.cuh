@@ -48,6 +48,7 @@ struct SolveResult {
     double rel_residual = 0.0;
     double iter_residual = 0.0;
     double ms = 0.0;
+    int fallback = 0;  // mixed: the FP32 inner iterations failed, finished in FP64
 };
 
 // Matrix owned on the device in the block-row layout.  v32 is the FP32 copy
@@ -95,6 +96,11 @@ inline SellView<float> DevMatrix::sell<float>() const { return SellView<float>{n
 // values when stale.  Implemented in sell.cu.
 void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st);
 
+// Inverse of every diagonal block (PFG_PC_BLOCK_JACOBI) or diagonal entry
+// (PFG_PC_JACOBI) of A into d64 (and d32 unless null), BS*BS values per block
+// row.  Implemented in krylov.cu.
+void block_jacobi(const DevMatrix &A, int precond, double *d64, float *d32, cudaStream_t st);
+
 class Krylov {
   public:
     Krylov();
@@ -129,6 +135,7 @@ class Krylov {
     int bs_ = 3;
     // FP64 work vectors
     DevBuf<double> r_, r0_, z_, pA_, pB_, q_, yA_, yB_, e_, v_, dinv_, ph_, eh_;
+    DevBuf<double> xb_;  // mixed: x before the fold of an FP32 correction
     // FP32 work vectors
     DevBuf<float> r32_, r032_, z32_, pA32_, pB32_, q32_, yA32_, yB32_, e32_, v32_, x32_, dinv32_, ph32_, eh32_;
     DevBuf<double> partials_;

@@ -249,6 +249,7 @@ extern "C" int pfg_linear_solver_crs_noalloc(const int64_t *d_row_ptr, const int
             info->rel_residual = h.bb > 0 ? std::sqrt(h.rr / h.bb) : std::sqrt(h.rr);
             info->iter_residual = info->rel_residual;
             info->solve_ms = ms;
+            info->fallback = 0;
         }
     });
     if (rc != PFG_OK) return rc;

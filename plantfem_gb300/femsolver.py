@@ -213,6 +213,38 @@ class FEMSolver:
         self.last_info = info.as_dict()
         return x
 
+    def eliminate(self):
+        """Apply the Dirichlet elimination of FEMSolver_%solve (FEMSolverClass.f90:1707-1756)
+        to the stored matrix and RHS now (solve() does it itself)."""
+        N.check(self._lib.pfg_eliminate(self._h))
+
+    def getElementCauchyStress(self, displacement, E, v, option: str | None = None):
+        """getElementCauchyStress (FEMDomainClass.f90:15249): cell-averaged stress per
+        element; option None -> (ne, 3, 3) tensors, "I1" -> trace, "p" -> trace / 3."""
+        d = _f64(displacement)
+        Ev = _f64(np.atleast_1d(E))
+        vv = _f64(np.broadcast_to(np.atleast_1d(v), Ev.shape))
+        ne = self.domain.ne()
+        opt = {None: 0, "I1": 1, "I": 1, "trace": 1, "p": 2, "P": 2}[option]
+        out = np.zeros(ne * 9 if opt == 0 else ne)
+        N.check(self._lib.pfg_element_stress(self._h, N.ptr(d), Ev.shape[0], N.ptr(Ev), N.ptr(vv), opt, N.ptr(out)))
+        return out.reshape(ne, 3, 3) if opt == 0 else out
+
+    # device-array forms (PyTorch tensors)
+    def assembleStiffness_device(self, E, nu):
+        _torch_sync()
+        N.check(self._lib.pfg_dev_assemble_stiffness(self._h, E.numel(), E.data_ptr(), nu.data_ptr(), None))
+
+    def setRHS_device(self, rhs):
+        _torch_sync()
+        N.check(self._lib.pfg_dev_set_rhs(self._h, rhs.numel(), rhs.data_ptr(), None))
+
+    def adjoint_grad_E_device(self, u, lam, nu, grad):
+        _torch_sync()
+        N.check(self._lib.pfg_dev_adjoint_grad_E(self._h, u.data_ptr(), lam.data_ptr(), nu.numel(), nu.data_ptr(),
+                                                 grad.data_ptr(), None))
+        return grad
+
     # ------------------------------------------------------------ eigenproblem
     def keepThisMatrixAs(self, As: str):
         """FEMSolver_%keepThisMatrixAs (FEMSolverClass.f90:1544-1604)."""

@@ -46,4 +46,5 @@ def test_slab_problem_shapes():
     p = problems.slab(int(nx[0]), int(ny[0]), int(nz[0]), 1e4)
     d = p["domain"]
     assert abs(max(d.x_max(), d.y_max()) - 1.0) < 1e-12
-    assert p["fix_ids"].shape[0] == 3 * (min(nx[0], ny[0]) * 0 + (nz[0] + 1) * ((ny[0] if nx[0] <= ny[0] else nx[0]) + 1))
+    # the clamped face spans the short in-plane edge and the thickness
+    assert p["fix_ids"].shape[0] == 3 * (nz[0] + 1) * (min(nx[0], ny[0]) + 1)
