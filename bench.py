@@ -10,8 +10,11 @@ and boundary conditions resident in HBM to x at the tolerance):
 
 Reported next to it (same JSON line): the plain FP64 GPU solve, the FP64 and
 FP32 block SpMV bandwidth, the end-to-end solve through the C ABI's
-LinearSolver plug-in with host CRS arrays, and the CPU oracle port of the
-reference's bicgstab_CRS_2 timed on the host cores.
+LinearSolver plug-in with host CRS arrays, the CPU oracle port of the
+reference's bicgstab_CRS_2 timed on the host cores, and the two other forms
+against the plain path on the same GPU: 512 uneven thin slabs solved in one
+persistent batched launch (``batched_slabs``) and the adjoint dL/dE of a 64^3
+mesh with 262,144 per-element moduli (``adjoint``).
 
 ``--impl reference`` times the reference algorithm itself on the host CPU
 (the oracle's restatement of bicgstab_CRS_2 with the per-nonzero OpenMP
@@ -296,6 +299,135 @@ def modal_lines(n=60, nev=20, block=24, tol=1e-8):
     return out
 
 
+def batch_lines(count=512, tol=1e-8, seed=5):
+    """Batched uneven organs: `count` thin slabs nx x ny x nz (nx, ny ~ U{8..64},
+    nz ~ U{1..3}, numpy seed 5), E lognormal per slab, nu 0.3, one short edge
+    clamped, transverse traction -1; all solved in ONE persistent graph-replayed
+    launch (pfg_batch_solve), FP64 and mixed, to a true relative residual of
+    `tol`, with the autotuned launch configuration; against the plain path
+    (FEMSolver_%solve on each slab in turn) on the same GPU."""
+    from plantfem_gb300 import FEMSolver, FEMSolverBatch, problems
+    nx, ny, nz, rng = problems.slab_sizes(count, seed=seed)
+    Es = np.exp(rng.normal(np.log(1e4), 0.5, size=count))
+    t0 = time.perf_counter()
+    solvers = []
+    for k in range(count):
+        p = problems.slab(int(nx[k]), int(ny[k]), int(nz[k]), Es[k])
+        sv = FEMSolver()
+        sv.setDomain(p["domain"])
+        sv.setCRS(3)
+        sv.assembleStiffness(p["E"], p["nu"])
+        sv.setRHS(p["rhs"])
+        sv.fix(1, p["fix_ids"], FixValue=0.0)
+        solvers.append(sv)
+    t_build = time.perf_counter() - t0
+    B = FEMSolverBatch(solvers)
+    dofs = [sv.ndof() for sv in solvers]
+    out = {"workload": f"{count} slabs, {sum(dofs)} DOF in total ({min(dofs)}..{max(dofs)} per slab), "
+                       f"CG + 3x3 block Jacobi, true relative residual {tol:g}",
+           "setup_s": round(t_build, 2)}
+    xs64 = None
+    for prec in ("fp64", "mixed"):
+        cfg, tune_ms = B.tune(precision=prec, relative_er=tol)
+        ms = []
+        for _ in range(3):
+            xs = B.solve(precision=prec, relative_er=tol)
+            ms.append(B.last_info["solve_ms"])
+        inf = B.last_info
+        st = [i["status"] for i in B.last_infos]
+        out[f"batched_{prec}"] = {"ms": round(min(ms), 2), "ms_runs": [round(v, 2) for v in ms],
+                                  "launches": inf["launches"], "config": cfg,
+                                  "max_iterations": inf["max_iterations"],
+                                  "total_iterations": inf["total_iterations"],
+                                  "max_rel_residual": inf["max_rel_residual"], "fp64_systems": inf["fallbacks"],
+                                  "converged": st.count(0)}
+        if prec == "fp64":
+            xs64 = xs
+        else:
+            out["max_rel_diff_mixed_vs_fp64"] = float(max(np.linalg.norm(a - c) / np.linalg.norm(c)
+                                                          for a, c in zip(xs, xs64)))
+        _progress(f"batched {prec}: {min(ms):.1f} ms")
+    for prec in ("fp64", "mixed"):
+        t_a = time.perf_counter()
+        dev = 0.0
+        worst = 0.0
+        fb = 0
+        for k, sv in enumerate(solvers):
+            sv.relative_er = tol
+            xk = sv.solve(algorithm="CG", preconditioning="BlockJacobi", precision=prec, stop_rule="true_relative")
+            dev += sv.last_info["solve_ms"]
+            fb += sv.last_info["fallback"]
+            worst = max(worst, float(np.linalg.norm(xk - xs64[k]) / np.linalg.norm(xs64[k])))
+        wall = (time.perf_counter() - t_a) * 1e3
+        out[f"plain_{prec}"] = {"ms": round(dev, 1), "wall_ms": round(wall, 1), "fp64_fallbacks": fb,
+                                "max_rel_diff_vs_batched_fp64": worst}
+        out[f"speedup_batched_vs_plain_{prec}"] = round(dev / out[f"batched_{prec}"]["ms"], 2)
+        _progress(f"plain {prec}: {dev:.1f} ms")
+    del B
+    for sv in solvers:
+        sv.remove()
+    return out
+
+
+def adjoint_lines(n=64, n_fd=32, tol=1e-10):
+    """Adjoint stiffness identification: n^3 hex mesh with one lognormal E per
+    element (numpy seed 2), loss 0.5 |u(E) - u_t|^2 with u_t solved from a
+    second field (seed 1); dL/dE for every element by one adjoint solve
+    (torch.autograd.Function), checked by central differences (h = 1e-4 E) on
+    n_fd elements drawn with seed 3; FP64 and mixed; against the plain forward
+    solve."""
+    import torch
+    from plantfem_gb300 import problems
+    from plantfem_gb300.adjoint import ElasticOperator
+    p = problems.lognormal(n, seed=2)  # the parameter field E
+    dom = p["domain"]
+    ne = dom.ne()
+    E_t = problems.lognormal_E(ne, seed=1)  # the field u_t is solved from
+    dev = torch.device("cuda", torch.cuda.current_device())
+    out = {"workload": f"lognormal{n}: {3 * dom.nn()} DOF, {ne} per-element E, loss 0.5|u-u_t|^2, CG + block "
+                       f"Jacobi to {tol:g}, central FD h=1e-4 E on {n_fd} elements"}
+    grads = {}
+    for prec in ("fp64", "mixed"):
+        op = ElasticOperator(dom, p["nu"], p["rhs"], p["fix_ids"], precision=prec, relative_er=tol)
+        with torch.no_grad():
+            u_t = op.displacement(torch.tensor(E_t, device=dev))
+        Et = torch.tensor(p["E"], device=dev, requires_grad=True)
+        op.displacement(Et.detach())  # warm-up: graphs and buffers
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        u = op.displacement(Et)
+        L = 0.5 * torch.sum((u - u_t) ** 2)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        L.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        g = Et.grad.detach().cpu().numpy()
+        grads[prec] = g
+        out[prec] = {"forward_ms": round((t1 - t0) * 1e3, 2), "backward_ms": round((t2 - t1) * 1e3, 2),
+                     "backward_vs_forward": round((t2 - t1) / (t1 - t0), 3), "loss": float(L.detach())}
+        if prec == "fp64":
+            rng = np.random.default_rng(3)
+            ks = rng.choice(ne, size=n_fd, replace=False)
+            errs = []
+            for k in ks:
+                h = 1e-4 * p["E"][k]
+                Ls = []
+                for sgn in (1.0, -1.0):
+                    Ek = p["E"].copy()
+                    Ek[k] += sgn * h
+                    with torch.no_grad():
+                        uk = op.displacement(torch.tensor(Ek, device=dev))
+                    Ls.append(0.5 * float(torch.sum((uk - u_t) ** 2)))
+                errs.append(abs((Ls[0] - Ls[1]) / (2 * h) - g[k]))
+            out["fd_check"] = {"elements": n_fd, "max_abs_err_over_max_grad": float(max(errs) / np.abs(g).max())}
+        _progress(f"adjoint {prec} done")
+        del op
+    out["max_rel_grad_diff_mixed_vs_fp64"] = float(np.abs(grads["mixed"] - grads["fp64"]).max()
+                                                   / np.abs(grads["fp64"]).max())
+    return out
+
+
 def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_mixed, ms_step, value, f64_infos,
              ms_f64, clk, setup_s, t0, t_pat, t_asm, out_extra):
     import torch
@@ -355,6 +487,16 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
 
     if args.modal and rank == 0:
         out_extra["modal_lobpcg"] = modal_lines(args.modal_n)
+    if not args.skip_batch and rank == 0:
+        try:
+            out_extra["batched_slabs"] = batch_lines(args.batch_count)
+        except Exception as e:
+            out_extra["batched_slabs"] = {"error": str(e)}
+    if not args.skip_adjoint and rank == 0:
+        try:
+            out_extra["adjoint"] = adjoint_lines()
+        except Exception as e:
+            out_extra["adjoint"] = {"error": str(e)}
     launches = int(sum(i["kernel_launches"] for i in infos))
     line = {
         "metric": "solves/s of the 3,090,903-DOF hex8 elasticity solve at 1e-10 relative residual "
@@ -364,7 +506,8 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
         "dtype": "f32 inner / f64 residual", "data": "synthetic (seeded lognormal E, numpy seed 20261203)",
         "config": {"workload": f"lognormal{n}: Cube3D {n}^3 hex8, {ndof} DOF, E~lognormal(ln1e4, 0.5), nu 0.3, "
                                "z=0 fixed, top traction -1; CG + 3x3 block Jacobi; rel. residual 1e-10",
-                   "l2": "inputs larger than L2 (FP32 matrix 1.1 GB read per SpMV)",
+                   "l2": f"inputs larger than L2 (FP32 matrix {prof['spmv_fp32']['bytes'] / 1e9:.2f} GB read "
+                         "per SpMV)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "mixed": {"iterations": mixed_info["iterations"], "replacements": mixed_info["replacements"],
                   "rel_residual": mixed_info["rel_residual"], "rel_err_vs_fp64": err_mixed,
@@ -478,6 +621,9 @@ def main():
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--modal", action="store_true", help="also run the LOBPCG modal analysis (FP64 vs mixed)")
     ap.add_argument("--modal-n", type=int, default=60)
+    ap.add_argument("--skip-batch", action="store_true", help="skip the 512-slab batched solve lines")
+    ap.add_argument("--batch-count", type=int, default=512, help="slabs in the batched solve lines")
+    ap.add_argument("--skip-adjoint", action="store_true", help="skip the 64^3 adjoint lines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -46,5 +46,6 @@ def test_slab_problem_shapes():
     p = problems.slab(int(nx[0]), int(ny[0]), int(nz[0]), 1e4)
     d = p["domain"]
     assert abs(max(d.x_max(), d.y_max()) - 1.0) < 1e-12
-    # the clamped face spans the short in-plane edge and the thickness
-    assert p["fix_ids"].shape[0] == 3 * (nz[0] + 1) * (min(nx[0], ny[0]) + 1)
+    # clamped face x = 0 (y = 0 when nx > ny): it spans the longer in-plane
+    # edge and the thickness
+    assert p["fix_ids"].shape[0] == 3 * (nz[0] + 1) * (max(nx[0], ny[0]) + 1)
