@@ -45,17 +45,16 @@ constexpr int kMaxStall = 3;
 constexpr float kDiverge = 1.0e3f;
 
 struct TeamShared {
-    double slot[2][kMaxCluster][4];   // per-rank partials of team reductions (rank 0's copy is used)
-    double red[4 * 32];               // block reduction scratch (FP64)
-    float red32[2 * 4 * 32];          // block reduction scratch (compensated FP32)
-    double bc[4];                     // reduced values broadcast to the CTA
+    double slot[2][kMaxCluster][4];   // CTA totals of team reductions, one row per rank (every CTA holds all)
+    double wpart[2][32][4];           // per-warp partials (FP64), double-buffered
+    float wpart32[2][32][4];          // per-warp compensated partials (s, c pairs), double-buffered
     int job;
 };
 
 struct Team {
     int rank;   // CTA rank in the team
     int size;   // CTAs in the team (1: a single CTA, no cluster barrier)
-    int nred;   // reductions done on this job (alternates the slot buffers)
+    int nred;   // reductions done on this job (alternates the double buffers)
 };
 
 __device__ __forceinline__ void team_sync(const Team &tm)
@@ -66,51 +65,80 @@ __device__ __forceinline__ void team_sync(const Team &tm)
         __syncthreads();
 }
 
-// Team-wide sums of NV FP64 values; every thread of every CTA of the team gets
-// the same bits (partials are added in rank order by the same butterfly).
+// Team-wide sums of NV FP64 values with one CTA barrier (plus one cluster
+// barrier in a cluster team).  Every warp forms the CTA total from the warp
+// partials with the same butterfly; in a cluster, lane r of warp 0 pushes the
+// CTA total into row `rank` of CTA r's slot table (distributed shared memory),
+// and after the cluster barrier every warp adds its own CTA's copy of the table
+// in rank order -- all threads of the team get the same bits and no thread
+// reads remote shared memory.  The buffers alternate between consecutive
+// reductions: a buffer is rewritten two reductions later, after every thread
+// has passed the barrier of the reduction in between, i.e. after every thread
+// has read it.
 template <int NV>
 __device__ __forceinline__ void team_sum(double (&v)[NV], Team &tm, TeamShared &sh)
 {
     static_assert(NV <= 4, "at most 4 values per reduction");
-    block_sum<NV>(v, sh.red);  // warp 0 holds the CTA totals
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int buf = tm.nred++ & 1;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh.wpart[buf][wid][k] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = warp_sum(lane < nw ? sh.wpart[buf][lane][k] : 0.0);
     if (tm.size > 1) {
         cg::cluster_group cl = cg::this_cluster();
-        if (threadIdx.x == 0) {
-            double *dst = cl.map_shared_rank(&sh.slot[buf][tm.rank][0], 0);
+        if (wid == 0 && lane < tm.size) {
+            double *dst = cl.map_shared_rank(&sh.slot[buf][tm.rank][0], lane);
 #pragma unroll
             for (int k = 0; k < NV; ++k) dst[k] = v[k];
         }
         cl.sync();
-        if (threadIdx.x < 32) {
-            const double *src = cl.map_shared_rank(&sh.slot[buf][0][0], 0);
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                double t = (int)threadIdx.x < tm.size ? src[threadIdx.x * 4 + k] : 0.0;
-                t = warp_sum(t);
-                if (threadIdx.x == 0) sh.bc[k] = t;
-            }
-        }
-    } else if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sh.bc[k] = v[k];
+        for (int k = 0; k < NV; ++k) v[k] = warp_sum(lane < tm.size ? sh.slot[buf][lane][k] : 0.0);
     }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] = sh.bc[k];
 }
 
-// Team-wide compensated FP32 sums (Dot2 accumulators), rounded to float at the end.
+__device__ __forceinline__ void comp_warp_merge(Comp32 &t)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, t.s, o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, t.c, o);
+        comp_merge(t, s2, c2);
+    }
+}
+
+// Team-wide compensated FP32 sums (Dot2 accumulators), rounded to float at the
+// end; same structure as team_sum.
 template <int NV>
 __device__ __forceinline__ void team_sum_comp(Comp32 (&v)[NV], float (&tot)[NV], Team &tm, TeamShared &sh)
 {
     static_assert(NV <= 2, "at most 2 compensated values per reduction");
-    block_sum_comp<NV>(v, sh.red32);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int buf = tm.nred++ & 1;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) comp_warp_merge(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            sh.wpart32[buf][wid][2 * k] = v[k].s;
+            sh.wpart32[buf][wid][2 * k + 1] = v[k].c;
+        }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        v[k].s = lane < nw ? sh.wpart32[buf][lane][2 * k] : 0.f;
+        v[k].c = lane < nw ? sh.wpart32[buf][lane][2 * k + 1] : 0.f;
+        comp_warp_merge(v[k]);
+    }
     if (tm.size > 1) {
         cg::cluster_group cl = cg::this_cluster();
-        if (threadIdx.x == 0) {
-            double *dst = cl.map_shared_rank(&sh.slot[buf][tm.rank][0], 0);
+        if (wid == 0 && lane < tm.size) {
+            double *dst = cl.map_shared_rank(&sh.slot[buf][tm.rank][0], lane);
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 dst[2 * k] = (double)v[k].s;
@@ -118,30 +146,15 @@ __device__ __forceinline__ void team_sum_comp(Comp32 (&v)[NV], float (&tot)[NV],
             }
         }
         cl.sync();
-        if (threadIdx.x < 32) {
-            const double *src = cl.map_shared_rank(&sh.slot[buf][0][0], 0);
 #pragma unroll
-            for (int k = 0; k < NV; ++k) {
-                Comp32 t;
-                const bool in = (int)threadIdx.x < tm.size;
-                t.s = in ? (float)src[threadIdx.x * 4 + 2 * k] : 0.f;
-                t.c = in ? (float)src[threadIdx.x * 4 + 2 * k + 1] : 0.f;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const float s2 = __shfl_xor_sync(0xffffffffu, t.s, o);
-                    const float c2 = __shfl_xor_sync(0xffffffffu, t.c, o);
-                    comp_merge(t, s2, c2);
-                }
-                if (threadIdx.x == 0) sh.bc[k] = (double)__fadd_rn(t.s, t.c);
-            }
+        for (int k = 0; k < NV; ++k) {
+            v[k].s = lane < tm.size ? (float)sh.slot[buf][lane][2 * k] : 0.f;
+            v[k].c = lane < tm.size ? (float)sh.slot[buf][lane][2 * k + 1] : 0.f;
+            comp_warp_merge(v[k]);
         }
-    } else if (threadIdx.x == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sh.bc[k] = (double)__fadd_rn(v[k].s, v[k].c);
     }
-    __syncthreads();
 #pragma unroll
-    for (int k = 0; k < NV; ++k) tot[k] = (float)sh.bc[k];
+    for (int k = 0; k < NV; ++k) tot[k] = __fadd_rn(v[k].s, v[k].c);
 }
 
 // Abort flag of the batch, read by rank 0 and agreed on by the team.
@@ -270,8 +283,15 @@ __device__ void restore_fixed_rows(const BatchMesh &D, const Span &sp, int64_t n
 }
 
 // ------------------------------------------------------------- FP64 CG
-// CG on K x = b from the current x (true residual first), counting on from
-// `it`; returns the status, `rel` = true |b - Kx| / |b| at exit.
+// Chronopoulos-Gear CG (one reduction of three dot products per iteration)
+// on K x = b from the current x, counting on from `it`:
+//   x += a p, r -= a s, u = M^-1 r        (own rows, p = u + b p, s = w + b s first)
+//   w = K u ; g = <r,u>, d = <w,u>, rr = <r,r>       -> one team reduction
+//   b = g / g_old, a = g / (d - b g / a_old)
+// so an iteration synchronises the team twice: u complete before the gathers,
+// and the reduction.  A recursive residual at the tolerance is confirmed on
+// the true residual (restart from it otherwise, at most P.max_restarts).
+// Returns the status; `rel` = true |b - Kx| / |b| at exit.
 template <int NT>
 __device__ int cg64(const BatchParams &P, const BatchMesh &D, Team &tm, TeamShared &sh, int &it, int &restarts,
                     double &rel)
@@ -281,148 +301,138 @@ __device__ int cg64(const BatchParams &P, const BatchMesh &D, Team &tm, TeamShar
     const int lane = threadIdx.x & 31;
     const Span sp = team_span(tm, NT / 32);
     const int pc = P.precond;
+    const bool lead = tm.rank == 0 && threadIdx.x == 0;
 
-    // r = b - K x0, z = M^-1 r, p = z
-    double a3[3] = {0.0, 0.0, 0.0};
-    for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
-        double y[3];
-        sell_row_product<3>(A, s, lane, GatherCG<double>{D.x}, y);
-        const int64_t row = s * 32 + lane;
-        if (row < nb) {
-            double rv[3], zv[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const double bi = __ldg(D.b + 3 * row + k);
-                rv[k] = bi - y[k];
-                a3[2] = fma(bi, bi, a3[2]);
-            }
-            precond3<double>(pc, D.dinv64, row, rv, zv);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int64_t i = 3 * row + k;
-                D.r64[i] = rv[k];
-                D.z64[i] = zv[k];
-                D.p64[i] = zv[k];
-                a3[0] = fma(rv[k], zv[k], a3[0]);
-                a3[1] = fma(rv[k], rv[k], a3[1]);
-            }
-        }
-    }
-    team_sum<3>(a3, tm, sh);  // also completes p for the first gathers
-    double rho = a3[0], rr = a3[1];
-    const double bb = a3[2];
-    const double tol_b = P.tol * sqrt(bb);
-    int status = PFG_OK;
-    rel = bb > 0.0 ? sqrt(rr / bb) : 0.0;
-    bool converged = sqrt(rr) <= tol_b;
-    while (!converged) {
-        if (it >= P.itrmax) {
-            status = PFG_W_NOT_CONVERGED;
-            break;
-        }
-        if (P.abort && it % kAbortEvery == 0 && team_abort(P, tm, sh)) {
-            status = PFG_E_ABORTED;
-            break;
-        }
-        // q = K p, <p, q>
-        double a1[1] = {0.0};
+    // r = b - K x0 and |b|^2
+    double bb;
+    {
+        double a2[2] = {0.0, 0.0};
         for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
             double y[3];
-            sell_row_product<3>(A, s, lane, GatherCG<double>{D.p64}, y);
+            sell_row_product<3>(A, s, lane, GatherCG<double>{D.x}, y);
             const int64_t row = s * 32 + lane;
             if (row < nb)
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int64_t i = 3 * row + k;
-                    D.q64[i] = y[k];
-                    a1[0] = fma(D.p64[i], y[k], a1[0]);
+                    const double bi = __ldg(D.b + i);
+                    const double rv = bi - y[k];
+                    D.r64[i] = rv;
+                    a2[0] = fma(rv, rv, a2[0]);
+                    a2[1] = fma(bi, bi, a2[1]);
                 }
         }
-        team_sum<1>(a1, tm, sh);
-        if (!(a1[0] > 0.0) || !isfinite(a1[0])) {
-            status = PFG_E_BREAKDOWN;
-            break;
-        }
-        const double alpha = rho / a1[0];
-        // x += alpha p, r -= alpha q, z = M^-1 r, <r, z>, <r, r>
-        double a2[2] = {0.0, 0.0};
+        team_sum<2>(a2, tm, sh);
+        bb = a2[1];
+        rel = bb > 0.0 ? sqrt(a2[0] / bb) : 0.0;
+        if (sqrt(a2[0]) <= P.tol * sqrt(bb)) return PFG_OK;
+    }
+    const double tol_b = P.tol * sqrt(bb);
+    int status = PFG_OK;
+    bool fresh = true;   // (re)start: the next direction update is p = u, s = w
+    double alpha = 0.0, beta = 0.0, gamma = 0.0;
+    for (;;) {
+        // own rows: direction update, x and r, u = M^-1 r
         for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
             const int64_t row = s * 32 + lane;
             if (row >= nb) continue;
             double rv[3], zv[3];
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int64_t i = 3 * row + k;
-                D.x[i] = fma(alpha, D.p64[i], D.x[i]);
-                rv[k] = fma(-alpha, D.q64[i], D.r64[i]);
-                D.r64[i] = rv[k];
+            for (int k = 0; k < 3; ++k) rv[k] = D.r64[3 * row + k];
+            if (!fresh) {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int64_t i = 3 * row + k;
+                    const double pv = fma(beta, D.p64[i], D.z64[i]);
+                    const double sv = fma(beta, D.s64[i], D.q64[i]);
+                    D.p64[i] = pv;
+                    D.s64[i] = sv;
+                    D.x[i] = fma(alpha, pv, D.x[i]);
+                    rv[k] = fma(-alpha, sv, rv[k]);
+                    D.r64[i] = rv[k];
+                }
             }
             precond3<double>(pc, D.dinv64, row, rv, zv);
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                D.z64[3 * row + k] = zv[k];
-                a2[0] = fma(rv[k], zv[k], a2[0]);
-                a2[1] = fma(rv[k], rv[k], a2[1]);
-            }
+            for (int k = 0; k < 3; ++k) D.z64[3 * row + k] = zv[k];
         }
-        team_sum<2>(a2, tm, sh);  // x complete for a true residual
-        ++it;
-        if (!isfinite(a2[0]) || !isfinite(a2[1])) {
+        team_sync(tm);  // u complete before the gathers
+        // w = K u ; <r,u>, <w,u>, <r,r>, and the abort flag every kAbortEvery iterations
+        double a4[4] = {0.0, 0.0, 0.0, 0.0};
+        if (P.abort && lead && it % kAbortEvery == 0) a4[3] = (double)(*P.abort != 0);
+        for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
+            double y[3];
+            sell_row_product<3>(A, s, lane, GatherCG<double>{D.z64}, y);
+            const int64_t row = s * 32 + lane;
+            if (row < nb)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int64_t i = 3 * row + k;
+                    const double uv = D.z64[i], rv = D.r64[i];
+                    D.q64[i] = y[k];
+                    a4[0] = fma(rv, uv, a4[0]);
+                    a4[1] = fma(y[k], uv, a4[1]);
+                    a4[2] = fma(rv, rv, a4[2]);
+                }
+        }
+        team_sum<4>(a4, tm, sh);
+        if (!fresh) ++it;
+        if (a4[3] != 0.0) {
+            status = PFG_E_ABORTED;
+            break;
+        }
+        if (!isfinite(a4[0]) || !isfinite(a4[1]) || !isfinite(a4[2])) {
             status = PFG_E_NONFINITE;
             break;
         }
-        double beta;
-        if (sqrt(a2[1]) <= tol_b) {
-            // recursive residual converged: confirm on the true residual
+        const double g = a4[0], d = a4[1];
+        double a_new = 0.0, b_new = 0.0;
+        if (fresh) {
+            a_new = g / d;
+        } else {
+            b_new = g / gamma;
+            a_new = g / (d - b_new * g / alpha);
+        }
+        const bool broke = !(a_new > 0.0) || !isfinite(a_new);
+        if (sqrt(a4[2]) <= tol_b || broke) {
+            // recursive residual at the tolerance (or a breakdown of the
+            // recurrences): decide on the true residual, restart from it if
+            // needed (x is complete: its rows were written before the reduction)
             const double rt = residual64(D, sp, tm, sh);
             rel = bb > 0.0 ? sqrt(rt / bb) : 0.0;
-            if (sqrt(rt) <= tol_b) {
-                converged = true;
-                break;
-            }
+            if (sqrt(rt) <= tol_b) return PFG_OK;
             if (restarts >= P.max_restarts) {
-                status = PFG_W_NOT_CONVERGED;
+                status = broke ? PFG_E_BREAKDOWN : PFG_W_NOT_CONVERGED;
                 break;
             }
             ++restarts;
-            // restart from the true residual (r64 holds it): z = M^-1 r, p = z
-            double ar[1] = {0.0};
+            fresh = true;  // restart from the true residual now in r64
+            continue;
+        }
+        if (it >= P.itrmax) {
+            status = PFG_W_NOT_CONVERGED;
+            break;
+        }
+        alpha = a_new;
+        beta = b_new;
+        gamma = g;
+        if (fresh) {
+            // p = u, s = w for the first update after a (re)start
             for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
                 const int64_t row = s * 32 + lane;
                 if (row >= nb) continue;
-                double rv[3], zv[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) rv[k] = D.r64[3 * row + k];
-                precond3<double>(pc, D.dinv64, row, rv, zv);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    D.z64[3 * row + k] = zv[k];
-                    ar[0] = fma(rv[k], zv[k], ar[0]);
+                    const int64_t i = 3 * row + k;
+                    D.p64[i] = 0.0;
+                    D.s64[i] = 0.0;
                 }
             }
-            team_sum<1>(ar, tm, sh);
-            rho = ar[0];
-            beta = 0.0;
-        } else {
-            beta = a2[0] / rho;
-            rho = a2[0];
+            fresh = false;
         }
-        // p = z + beta p
-        for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
-            const int64_t row = s * 32 + lane;
-            if (row >= nb) continue;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int64_t i = 3 * row + k;
-                D.p64[i] = beta == 0.0 ? D.z64[i] : fma(beta, D.p64[i], D.z64[i]);
-            }
-        }
-        team_sync(tm);
     }
-    if (!converged) {
-        const double rt = residual64(D, sp, tm, sh);
-        rel = bb > 0.0 ? sqrt(rt / bb) : 0.0;
-    }
+    const double rt = residual64(D, sp, tm, sh);
+    rel = bb > 0.0 ? sqrt(rt / bb) : 0.0;
     return status;
 }
 
@@ -795,7 +805,7 @@ struct pfg_batch {
     std::vector<BatchSource> src;
     std::vector<int64_t> ndof, off;   // DOF of each system and its offset in the pooled vectors
     int64_t total = 0;                // pooled length (each system padded to 32 values)
-    DevBuf<double> v64;               // x | r | p | q | z, `total` values each
+    DevBuf<double> v64;               // x | r | p | q | z | s, `total` values each
     DevBuf<float> v32;                // x32 | r32 | p32 | q32 | z32
     DevBuf<double> d64;               // block-Jacobi inverses, 3 * total
     DevBuf<float> d32;
@@ -1029,7 +1039,7 @@ int pfg_batch_set(pfg_batch *b, int64_t count, pfg_solver *const *handles)
             tot += (K.ndof() + 31) / 32 * 32;
         }
         b->total = tot;
-        b->v64.resize((size_t)tot * 5);
+        b->v64.resize((size_t)tot * 6);
         b->v32.resize((size_t)tot * 5);
         b->d64.resize((size_t)tot * 3);
         b->d32.resize((size_t)tot * 3);
@@ -1049,6 +1059,7 @@ int pfg_batch_set(pfg_batch *b, int64_t count, pfg_solver *const *handles)
             d.p64 = b->v64.p + 2 * tot + o;
             d.q64 = b->v64.p + 3 * tot + o;
             d.z64 = b->v64.p + 4 * tot + o;
+            d.s64 = b->v64.p + 5 * tot + o;
             d.x32 = b->v32.p + o;
             d.r32 = b->v32.p + tot + o;
             d.p32 = b->v32.p + 2 * tot + o;

@@ -44,7 +44,7 @@ struct BatchMesh {
     const uint8_t *fixed;
     const double *fixval;
     double *x;                            // x0 in, solution out
-    double *r64, *p64, *q64, *z64;        // FP64 work vectors
+    double *r64, *p64, *q64, *z64, *s64;  // FP64 work vectors (CG: r, p, w, u, s)
     float *x32, *r32, *p32, *q32, *z32;   // FP32 work vectors
     const double *dinv64;                 // block-Jacobi inverses (9 per block row)
     const float *dinv32;

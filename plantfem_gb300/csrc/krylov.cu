@@ -1390,9 +1390,11 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
     return res;
 }
 
-// Replacements in a row whose FP64 residual did not fall by 10 % before the
-// mixed solve hands over to FP64.
-constexpr int kMixedStall = 4;
+// Replacements in a row whose FP64 residual did not fall by 10 %, and FP32
+// passes in a row whose correction was rejected, before the mixed solve hands
+// over to FP64 (BiCGSTAB's residual is erratic: it gets more room).
+constexpr int kMixedStallCG = 4, kMixedStallBiCG = 8;
+constexpr int kMixedRejectCG = 2, kMixedRejectBiCG = 3;
 
 SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st)
 {
@@ -1478,7 +1480,7 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
         }
         prev_rel = rel;
         failures = rejected ? failures + 1 : 0;
-        if (failures >= 2 && rel > cfg.relative_er) {
+        if (failures >= (cg ? kMixedRejectCG : kMixedRejectBiCG) && rel > cfg.relative_er) {
             // two FP32 passes in a row made no progress: finish in FP64
             res.fallback = 1;
             res.iterations = h.iter;
@@ -1492,7 +1494,7 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
         if (first || rel < 0.9 * best_rel) {
             best_rel = rel;
             stall = 0;
-        } else if (++stall >= kMixedStall && rel > cfg.relative_er) {
+        } else if (++stall >= (cg ? kMixedStallCG : kMixedStallBiCG) && rel > cfg.relative_er) {
             res.fallback = 1;
             res.iterations = h.iter;
             res.replacements = h.replacements;
