@@ -335,8 +335,9 @@ int pfg_batch_get_x(pfg_batch *b, int64_t index, double *x_out);
 int pfg_batch_set_config(pfg_batch *b, const pfg_batch_config *cfg);
 int pfg_batch_get_config(pfg_batch *b, pfg_batch_config *cfg, int32_t *tuned);
 /* Autotuner: times full batched solves of the bound systems with `opts` over
- * candidate configurations (cluster size, then threads per CTA, then team
- * share), keeps the fastest for later solves and returns it. */
+ * candidate configurations (threads per CTA x cluster size, then the team
+ * share of the best), keeps the fastest for later solves and returns it;
+ * opts->debug prints every candidate's time. */
 int pfg_batch_tune(pfg_batch *b, const pfg_solve_opts *opts, pfg_batch_config *best, double *best_ms);
 /* Host address of the batch's abort flag (host-mapped memory, 0 at creation).
  * Setting it to 1 from any host thread makes every team retire its system with

@@ -51,9 +51,10 @@ class FEMSolverBatch:
         self._ndof = [s.ndof() for s in self.solvers]
         return self
 
-    def _opts(self, precision, preconditioning, relative_er, itrmax, reliable_delta):
+    def _opts(self, precision, preconditioning, relative_er, itrmax, reliable_delta, debug=False):
         o = N.default_opts(algorithm=N.ALG_CG, precision=_PREC[precision], precond=_PC[preconditioning],
-                           stop_rule=N.STOP_TRUE_RELATIVE, relative_er=float(relative_er), itrmax=int(itrmax))
+                           stop_rule=N.STOP_TRUE_RELATIVE, relative_er=float(relative_er), itrmax=int(itrmax),
+                           debug=int(bool(debug)))
         if reliable_delta is not None:
             o.reliable_delta = float(reliable_delta)
         return o
@@ -98,9 +99,10 @@ class FEMSolverBatch:
         N.check(self._lib.pfg_batch_set_config(self._h, C.byref(c)))
 
     def tune(self, precision: str = "mixed", preconditioning: str | None = "BlockJacobi",
-             relative_er: float = 1e-10, itrmax: int = 100000) -> tuple[dict, float]:
-        """Autotune the launch configuration on the bound systems; returns (config, ms)."""
-        o = self._opts(precision, preconditioning, relative_er, itrmax, None)
+             relative_er: float = 1e-10, itrmax: int = 100000, debug: bool = False) -> tuple[dict, float]:
+        """Autotune the launch configuration on the bound systems; returns (config, ms).
+        ``debug`` prints every candidate's time on stderr."""
+        o = self._opts(precision, preconditioning, relative_er, itrmax, None, debug)
         c = N.BatchConfig()
         ms = C.c_double()
         N.check(self._lib.pfg_batch_tune(self._h, C.byref(o), C.byref(c), C.byref(ms)))

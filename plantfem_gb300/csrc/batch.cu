@@ -209,19 +209,24 @@ __device__ __forceinline__ Span team_span(const Team &tm, int warps_per_cta)
 // Sum of squares of r = b - K x (FP64) over the team, r written out.
 __device__ double residual64(const BatchMesh &D, const Span &sp, Team &tm, TeamShared &sh)
 {
+    // Local copies of the descriptor's pointers: stores through them cannot
+    // alias the descriptor, so it is not re-read after every store.
     const int lane = threadIdx.x & 31;
-    const SellView<double> &A = D.A64;
+    const SellView<double> A = D.A64;
+    const double *__restrict__ b = D.b;
+    const double *__restrict__ x = D.x;
+    double *__restrict__ r = D.r64;
     double acc[1] = {0.0};
     for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
         double y[3];
-        sell_row_product<3>(A, s, lane, GatherCG<double>{D.x}, y);
+        sell_row_product<3>(A, s, lane, GatherCG<double>{x}, y);
         const int64_t row = s * 32 + lane;
         if (row < A.nb) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const int64_t i = 3 * row + k;
-                const double rv = __ldg(D.b + i) - y[k];
-                D.r64[i] = rv;
+                const double rv = __ldg(b + i) - y[k];
+                r[i] = rv;
                 acc[0] = fma(rv, rv, acc[0]);
             }
         }
@@ -247,18 +252,21 @@ struct GatherSum {
 __device__ double candidate_residual(const BatchMesh &D, const Span &sp, Team &tm, TeamShared &sh)
 {
     const int lane = threadIdx.x & 31;
-    const SellView<double> &A = D.A64;
+    const SellView<double> A = D.A64;
+    const double *__restrict__ b = D.b;
+    double *__restrict__ q = D.q64;
+    const GatherSum src{D.x, D.x32};
     double acc[1] = {0.0};
     for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
         double y[3];
-        sell_row_product<3>(A, s, lane, GatherSum{D.x, D.x32}, y);
+        sell_row_product<3>(A, s, lane, src, y);
         const int64_t row = s * 32 + lane;
         if (row < A.nb) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const int64_t i = 3 * row + k;
-                const double rv = __ldg(D.b + i) - y[k];
-                D.q64[i] = rv;
+                const double rv = __ldg(b + i) - y[k];
+                q[i] = rv;
                 acc[0] = fma(rv, rv, acc[0]);
             }
         }
@@ -269,7 +277,10 @@ __device__ double candidate_residual(const BatchMesh &D, const Span &sp, Team &t
 
 __device__ void restore_fixed_rows(const BatchMesh &D, const Span &sp, int64_t nb)
 {
-    if (!D.fixed) return;
+    const uint8_t *__restrict__ fixed = D.fixed;
+    const double *__restrict__ fixval = D.fixval;
+    double *__restrict__ x = D.x;
+    if (!fixed) return;
     const int lane = threadIdx.x & 31;
     for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
         const int64_t row = s * 32 + lane;
@@ -277,159 +288,195 @@ __device__ void restore_fixed_rows(const BatchMesh &D, const Span &sp, int64_t n
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 const int64_t i = 3 * row + k;
-                if (D.fixed[i]) D.x[i] = D.fixval[i];
+                if (fixed[i]) x[i] = fixval[i];
             }
     }
 }
 
 // ------------------------------------------------------------- FP64 CG
-// Chronopoulos-Gear CG (one reduction of three dot products per iteration)
-// on K x = b from the current x, counting on from `it`:
-//   x += a p, r -= a s, u = M^-1 r        (own rows, p = u + b p, s = w + b s first)
-//   w = K u ; g = <r,u>, d = <w,u>, rr = <r,r>       -> one team reduction
-//   b = g / g_old, a = g / (d - b g / a_old)
-// so an iteration synchronises the team twice: u complete before the gathers,
-// and the reduction.  A recursive residual at the tolerance is confirmed on
-// the true residual (restart from it otherwise, at most P.max_restarts).
-// Returns the status; `rel` = true |b - Kx| / |b| at exit.
+// Preconditioned CG on K x = b from the current x, counting on from `it`:
+//   q = K p, <p,q>                      -> team reduction (alpha)
+//   x += a p, r -= a q, z = M^-1 r, <r,z>, <r,r>   -> team reduction (beta, stop)
+//   p = z + b p                         -> team barrier (p complete for the gathers)
+// (The Chronopoulos-Gear form, one reduction per iteration, measured 8 % slower
+// here: its extra live vectors cost registers the SpMV needs.)  A recursive
+// residual at the tolerance is confirmed on the true residual, restarting from
+// it otherwise (at most P.max_restarts).  Returns the status; `rel` = true
+// |b - Kx| / |b| at exit.
 template <int NT>
 __device__ int cg64(const BatchParams &P, const BatchMesh &D, Team &tm, TeamShared &sh, int &it, int &restarts,
                     double &rel)
 {
-    const SellView<double> &A = D.A64;
+    const SellView<double> A = D.A64;
     const int64_t nb = A.nb;
     const int lane = threadIdx.x & 31;
     const Span sp = team_span(tm, NT / 32);
     const int pc = P.precond;
     const bool lead = tm.rank == 0 && threadIdx.x == 0;
 
-    // r = b - K x0 and |b|^2
-    double bb;
+    // r = b - K x0, z = M^-1 r, p = z
+    double a3[3] = {0.0, 0.0, 0.0};
     {
-        double a2[2] = {0.0, 0.0};
+        const double *__restrict__ b = D.b;
+        const double *__restrict__ x = D.x;
+        double *__restrict__ r = D.r64;
+        double *__restrict__ z = D.z64;
+        double *__restrict__ p = D.p64;
+        const double *__restrict__ dinv = D.dinv64;
         for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
             double y[3];
-            sell_row_product<3>(A, s, lane, GatherCG<double>{D.x}, y);
+            sell_row_product<3>(A, s, lane, GatherCG<double>{x}, y);
             const int64_t row = s * 32 + lane;
-            if (row < nb)
+            if (row < nb) {
+                double rv[3], zv[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double bi = __ldg(b + 3 * row + k);
+                    rv[k] = bi - y[k];
+                    a3[2] = fma(bi, bi, a3[2]);
+                }
+                precond3<double>(pc, dinv, row, rv, zv);
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int64_t i = 3 * row + k;
-                    const double bi = __ldg(D.b + i);
-                    const double rv = bi - y[k];
-                    D.r64[i] = rv;
-                    a2[0] = fma(rv, rv, a2[0]);
-                    a2[1] = fma(bi, bi, a2[1]);
+                    r[i] = rv[k];
+                    z[i] = zv[k];
+                    p[i] = zv[k];
+                    a3[0] = fma(rv[k], zv[k], a3[0]);
+                    a3[1] = fma(rv[k], rv[k], a3[1]);
                 }
+            }
         }
-        team_sum<2>(a2, tm, sh);
-        bb = a2[1];
-        rel = bb > 0.0 ? sqrt(a2[0] / bb) : 0.0;
-        if (sqrt(a2[0]) <= P.tol * sqrt(bb)) return PFG_OK;
     }
+    team_sum<3>(a3, tm, sh);  // also completes p for the first gathers
+    double rho = a3[0];
+    const double bb = a3[2];
     const double tol_b = P.tol * sqrt(bb);
     int status = PFG_OK;
-    bool fresh = true;   // (re)start: the next direction update is p = u, s = w
-    double alpha = 0.0, beta = 0.0, gamma = 0.0;
+    rel = bb > 0.0 ? sqrt(a3[1] / bb) : 0.0;
+    if (sqrt(a3[1]) <= tol_b) return PFG_OK;
     for (;;) {
-        // own rows: direction update, x and r, u = M^-1 r
-        for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
-            const int64_t row = s * 32 + lane;
-            if (row >= nb) continue;
-            double rv[3], zv[3];
-#pragma unroll
-            for (int k = 0; k < 3; ++k) rv[k] = D.r64[3 * row + k];
-            if (!fresh) {
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const int64_t i = 3 * row + k;
-                    const double pv = fma(beta, D.p64[i], D.z64[i]);
-                    const double sv = fma(beta, D.s64[i], D.q64[i]);
-                    D.p64[i] = pv;
-                    D.s64[i] = sv;
-                    D.x[i] = fma(alpha, pv, D.x[i]);
-                    rv[k] = fma(-alpha, sv, rv[k]);
-                    D.r64[i] = rv[k];
-                }
-            }
-            precond3<double>(pc, D.dinv64, row, rv, zv);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) D.z64[3 * row + k] = zv[k];
-        }
-        team_sync(tm);  // u complete before the gathers
-        // w = K u ; <r,u>, <w,u>, <r,r>, and the abort flag every kAbortEvery iterations
-        double a4[4] = {0.0, 0.0, 0.0, 0.0};
-        if (P.abort && lead && it % kAbortEvery == 0) a4[3] = (double)(*P.abort != 0);
-        for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
-            double y[3];
-            sell_row_product<3>(A, s, lane, GatherCG<double>{D.z64}, y);
-            const int64_t row = s * 32 + lane;
-            if (row < nb)
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const int64_t i = 3 * row + k;
-                    const double uv = D.z64[i], rv = D.r64[i];
-                    D.q64[i] = y[k];
-                    a4[0] = fma(rv, uv, a4[0]);
-                    a4[1] = fma(y[k], uv, a4[1]);
-                    a4[2] = fma(rv, rv, a4[2]);
-                }
-        }
-        team_sum<4>(a4, tm, sh);
-        if (!fresh) ++it;
-        if (a4[3] != 0.0) {
-            status = PFG_E_ABORTED;
-            break;
-        }
-        if (!isfinite(a4[0]) || !isfinite(a4[1]) || !isfinite(a4[2])) {
-            status = PFG_E_NONFINITE;
-            break;
-        }
-        const double g = a4[0], d = a4[1];
-        double a_new = 0.0, b_new = 0.0;
-        if (fresh) {
-            a_new = g / d;
-        } else {
-            b_new = g / gamma;
-            a_new = g / (d - b_new * g / alpha);
-        }
-        const bool broke = !(a_new > 0.0) || !isfinite(a_new);
-        if (sqrt(a4[2]) <= tol_b || broke) {
-            // recursive residual at the tolerance (or a breakdown of the
-            // recurrences): decide on the true residual, restart from it if
-            // needed (x is complete: its rows were written before the reduction)
-            const double rt = residual64(D, sp, tm, sh);
-            rel = bb > 0.0 ? sqrt(rt / bb) : 0.0;
-            if (sqrt(rt) <= tol_b) return PFG_OK;
-            if (restarts >= P.max_restarts) {
-                status = broke ? PFG_E_BREAKDOWN : PFG_W_NOT_CONVERGED;
-                break;
-            }
-            ++restarts;
-            fresh = true;  // restart from the true residual now in r64
-            continue;
-        }
         if (it >= P.itrmax) {
             status = PFG_W_NOT_CONVERGED;
             break;
         }
-        alpha = a_new;
-        beta = b_new;
-        gamma = g;
-        if (fresh) {
-            // p = u, s = w for the first update after a (re)start
+        // q = K p, <p, q>; the abort flag rides along every kAbortEvery iterations
+        double a2[2] = {0.0, 0.0};
+        if (P.abort && lead && it % kAbortEvery == 0) a2[1] = (double)(*P.abort != 0);
+        {
+            const double *__restrict__ p = D.p64;
+            double *__restrict__ q = D.q64;
+            for (int64_t s = sp.w0; s < A.ns; s += sp.nw) {
+                double y[3];
+                sell_row_product<3>(A, s, lane, GatherCG<double>{p}, y);
+                const int64_t row = s * 32 + lane;
+                if (row < nb)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const int64_t i = 3 * row + k;
+                        q[i] = y[k];
+                        a2[0] = fma(p[i], y[k], a2[0]);
+                    }
+            }
+        }
+        team_sum<2>(a2, tm, sh);
+        if (a2[1] != 0.0) {
+            status = PFG_E_ABORTED;
+            break;
+        }
+        if (!(a2[0] > 0.0) || !isfinite(a2[0])) {
+            status = PFG_E_BREAKDOWN;
+            break;
+        }
+        const double alpha = rho / a2[0];
+        // x += alpha p, r -= alpha q, z = M^-1 r, <r, z>, <r, r>
+        double a4[2] = {0.0, 0.0};
+        {
+            double *__restrict__ x = D.x;
+            double *__restrict__ r = D.r64;
+            double *__restrict__ z = D.z64;
+            const double *__restrict__ p = D.p64;
+            const double *__restrict__ q = D.q64;
+            const double *__restrict__ dinv = D.dinv64;
+            for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
+                const int64_t row = s * 32 + lane;
+                if (row >= nb) continue;
+                double rv[3], zv[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int64_t i = 3 * row + k;
+                    x[i] = fma(alpha, p[i], x[i]);
+                    rv[k] = fma(-alpha, q[i], r[i]);
+                    r[i] = rv[k];
+                }
+                precond3<double>(pc, dinv, row, rv, zv);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    z[3 * row + k] = zv[k];
+                    a4[0] = fma(rv[k], zv[k], a4[0]);
+                    a4[1] = fma(rv[k], rv[k], a4[1]);
+                }
+            }
+        }
+        team_sum<2>(a4, tm, sh);  // x complete for a true residual
+        ++it;
+        if (!isfinite(a4[0]) || !isfinite(a4[1])) {
+            status = PFG_E_NONFINITE;
+            break;
+        }
+        double beta;
+        if (sqrt(a4[1]) <= tol_b) {
+            // recursive residual converged: confirm on the true residual
+            const double rt = residual64(D, sp, tm, sh);
+            rel = bb > 0.0 ? sqrt(rt / bb) : 0.0;
+            if (sqrt(rt) <= tol_b) return PFG_OK;
+            if (restarts >= P.max_restarts) {
+                status = PFG_W_NOT_CONVERGED;
+                break;
+            }
+            ++restarts;
+            // restart from the true residual (r64 holds it): z = M^-1 r, p = z
+            double ar[1] = {0.0};
+            {
+                const double *__restrict__ r = D.r64;
+                double *__restrict__ z = D.z64;
+                const double *__restrict__ dinv = D.dinv64;
+                for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
+                    const int64_t row = s * 32 + lane;
+                    if (row >= nb) continue;
+                    double rv[3], zv[3];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) rv[k] = r[3 * row + k];
+                    precond3<double>(pc, dinv, row, rv, zv);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        z[3 * row + k] = zv[k];
+                        ar[0] = fma(rv[k], zv[k], ar[0]);
+                    }
+                }
+            }
+            team_sum<1>(ar, tm, sh);
+            rho = ar[0];
+            beta = 0.0;
+        } else {
+            beta = a4[0] / rho;
+            rho = a4[0];
+        }
+        // p = z + beta p (p = z after a restart)
+        {
+            double *__restrict__ p = D.p64;
+            const double *__restrict__ z = D.z64;
             for (int64_t s = sp.w0; s * 32 < nb; s += sp.nw) {
                 const int64_t row = s * 32 + lane;
                 if (row >= nb) continue;
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     const int64_t i = 3 * row + k;
-                    D.p64[i] = 0.0;
-                    D.s64[i] = 0.0;
+                    p[i] = beta == 0.0 ? z[i] : fma(beta, p[i], z[i]);
                 }
             }
-            fresh = false;
         }
+        team_sync(tm);
     }
     const double rt = residual64(D, sp, tm, sh);
     rel = bb > 0.0 ? sqrt(rt / bb) : 0.0;
@@ -467,7 +514,7 @@ template <int NT>
 __device__ void solve_mixed(const BatchParams &P, int m, Team &tm, TeamShared &sh)
 {
     const BatchMesh &D = P.mesh[m];
-    const SellView<float> &A = D.A32;
+    const SellView<float> A = D.A32;
     const int64_t nb = A.nb;
     const int lane = threadIdx.x & 31;
     const Span sp = team_span(tm, NT / 32);
@@ -683,7 +730,7 @@ __device__ __forceinline__ void solve_job(const BatchParams &P, int m, Team &tm,
 }
 
 template <bool MIXED, int NT>
-__global__ void __launch_bounds__(NT, 1024 / NT) k_batch_cg(BatchParams P)
+__global__ void __launch_bounds__(NT, 1) k_batch_cg(BatchParams P)
 {
     __shared__ TeamShared sh;
     if (P.cluster > 1) {
@@ -848,6 +895,7 @@ struct RunSpec {
     bool mixed;
     int precond, itrmax;
     double tol, delta;
+    int debug;
 };
 
 RunSpec run_spec(const pfg_solve_opts *opts)
@@ -868,7 +916,7 @@ RunSpec run_spec(const pfg_solve_opts *opts)
          "precond");
     need(o.itrmax > 0 && o.relative_er > 0.0, PFG_E_ARG, "itrmax and relative_er must be positive");
     need(o.reliable_delta > 0.0 && o.reliable_delta < 1.0, PFG_E_ARG, "reliable_delta must lie in (0, 1)");
-    return RunSpec{o.precision == PFG_PREC_MIXED, o.precond, o.itrmax, o.relative_er, o.reliable_delta};
+    return RunSpec{o.precision == PFG_PREC_MIXED, o.precond, o.itrmax, o.relative_er, o.reliable_delta, o.debug};
 }
 
 // Launches one batched solve with configuration c (graph replay when the
@@ -1183,28 +1231,26 @@ int pfg_batch_tune(pfg_batch *b, const pfg_solve_opts *opts, pfg_batch_config *b
             if (!valid_config(c)) return;
             if (persistent_grid(rs.mixed, c.threads, c.cluster) <= 0) return;
             const double ms = run_batch(b, rs, c);
+            if (rs.debug)
+                fprintf(stderr, "[pfg] batch tune: threads %d cluster %d team share %.4f: %.2f ms\n", c.threads,
+                        c.cluster, c.team_fraction, ms);
             if (ms < top_ms) {
                 top_ms = ms;
                 top = c;
             }
         };
-        // stage 1: team size; stage 2: CTA size (block rows per CTA tile); stage 3: team share
-        for (int cl : {1, 2, 4, 8}) {
-            pfg_batch_config c = cur;
-            c.cluster = cl;
-            trial(c);
-        }
-        cur = top;
-        for (int nt : {256, 512, 1024}) {
-            if (nt == cur.threads) continue;
-            pfg_batch_config c = cur;
-            c.threads = nt;
-            trial(c);
-        }
+        // stage 1: CTA size (block rows per CTA tile) x team size; stage 2: team share
+        for (int nt : {256, 512, 1024})
+            for (int cl : {1, 2, 4, 8}) {
+                pfg_batch_config c = cur;
+                c.threads = nt;
+                c.cluster = cl;
+                c.team_fraction = cl > 1 ? 0.125 : 0.0;
+                trial(c);
+            }
         cur = top;
         if (cur.cluster > 1)
-            for (double f : {0.0625, 0.125, 0.25, 0.5, 1.0}) {
-                if (f == cur.team_fraction) continue;
+            for (double f : {0.0625, 0.25, 0.5, 1.0}) {
                 pfg_batch_config c = cur;
                 c.team_fraction = f;
                 trial(c);
