@@ -693,6 +693,8 @@ ResInfo residuals(Ctx &c, Blocks<T> &B)
     return ri;
 }
 
+constexpr int kRefreshImages = 10;
+
 // One precision phase.  start: 0 random, 1 X already holds a start block.
 template <typename T>
 int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg, bool fp32_phase, int start,
@@ -712,7 +714,7 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
     apply_rr<T>(c, 1, B);
     bool haveP = false;
     double best = 1e300;
-    int since_best = 0;
+    int since_best = 0, since_refresh = 0;
     for (;;) {
         ResInfo ri = residuals<T>(c, B);
         max_rel = 0.0;
@@ -759,6 +761,18 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
         if (got < c.k) throw Error(PFG_E_BREAKDOWN, "LOBPCG: Rayleigh-Ritz basis lost rank");
         apply_rr<T>(c, nblk, B);
         haveP = true;
+        // The images KX, MX, KP, MP follow X and P through the same linear
+        // combinations; recompute them from X and P every kRefreshImages
+        // iterations so rounding in those updates cannot drift the residuals
+        // R = KX - MX Lambda away from the true ones (without this the FP64
+        // phase stalled near 3e-3 on the 60^3 cantilever).
+        if (++since_refresh >= kRefreshImages) {
+            since_refresh = 0;
+            spmm<T>(c, K, B.X.p, B.KX.p);
+            spmm<T>(c, M, B.X.p, B.MX.p);
+            spmm<T>(c, K, B.P.p, B.KP.p);
+            spmm<T>(c, M, B.P.p, B.MP.p);
+        }
     }
 }
 

@@ -257,7 +257,7 @@ class FEMSolver:
 
     def eig(self, num_eigen: int | None = None, block_size: int = 0, precision: str = "fp64",
             preconditioning: str | None = "BlockJacobi", stop_rule: str = "residual", seed: int = 1,
-            eigen_vectors: bool = True):
+            eigen_vectors: bool = True, tol_fp32: float | None = None):
         """(eigen_value, eigen_vectors) = FEMSolver_%eig (FEMSolverClass.f90:1384-1541).
 
         Always LOBPCG (LOBPCG_CRS, SparseClass.f90:2008-2239) on the matrices
@@ -276,6 +276,8 @@ class FEMSolver:
         o.stop_rule = {"reference": N.EIG_STOP_REFERENCE, "residual": N.EIG_STOP_RESIDUAL}[stop_rule]
         o.seed = int(seed)
         o.debug = int(bool(self.debug))
+        if tol_fp32 is not None:
+            o.tol_fp32 = float(tol_fp32)  # mixed: relative residual that ends the FP32 phase
         lam = np.zeros(nev)
         n = self.ndof()
         X = np.zeros((nev, n)) if eigen_vectors else None
