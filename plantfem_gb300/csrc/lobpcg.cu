@@ -694,6 +694,7 @@ ResInfo residuals(Ctx &c, Blocks<T> &B)
 }
 
 constexpr int kRefreshImages = 10;
+constexpr int kFp32Stall = 50;
 
 // One precision phase.  start: 0 random, 1 X already holds a start block.
 template <typename T>
@@ -713,7 +714,7 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
     if (rayleigh_ritz<T>(c, 1, B, rank_tol) < c.k) throw Error(PFG_E_BREAKDOWN, "LOBPCG: start block is rank deficient");
     apply_rr<T>(c, 1, B);
     bool haveP = false;
-    double best = 1e300;
+    double best = 1e300, best_lsum = 1e300;
     int since_best = 0, since_refresh = 0;
     for (;;) {
         ResInfo ri = residuals<T>(c, B);
@@ -731,11 +732,25 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
         if (conv) return 1;
         if (fp32_phase) {
             if (max_rel < cfg.tol_fp32) return 0;
-            if (max_rel < 0.9 * best) {
-                best = max_rel;
+            // FP32 floor: neither the mean log residual of the wanted pairs
+            // (by 10 %) nor the sum of their Ritz values (by more than FP32
+            // noise, 1e-6 relative) fell for kFp32Stall iterations.  From a
+            // random start the Ritz values fall for many iterations while the
+            // relative residuals grow, so the residuals alone are no signal.
+            double mlog = 0.0, lsum = 0.0;
+            for (int j = 0; j < cfg.nev; ++j) {
+                mlog += std::log(std::max(ri.rel[j], 1e-300));
+                lsum += c.hlam[j];
+            }
+            mlog /= cfg.nev;
+            const bool res_down = mlog < best - std::log(1.1);
+            const bool lam_down = lsum < best_lsum - 1e-6 * std::fabs(best_lsum);
+            if (res_down) best = mlog;
+            if (lam_down) best_lsum = lsum;
+            if (res_down || lam_down) {
                 since_best = 0;
-            } else if (++since_best > 30) {
-                return 0;  // FP32 floor reached
+            } else if (++since_best > kFp32Stall) {
+                return 0;
             }
         }
         if (iters_left <= 0) return -1;
