@@ -253,87 +253,109 @@ struct GramAcc<float> {
     __device__ double get() const { return (double)v.s + (double)v.c; }
 };
 
-constexpr int kGramRows = 16;
-constexpr int kMaxPairsPerThread = 19;  // m <= 96: 96*97/2 = 4656 pairs / 256 threads
+constexpr int kGramRows = 32;  // rows staged in shared memory per step
+constexpr int kGramSub = 4;    // each thread owns a 4 x 4 sub-tile of both Gram matrices
 
 // Upper triangles of S^T (K S) and S^T (M S), S = [X W P] (nblk blocks of k
-// columns): each CTA reduces a contiguous row range and writes its partial
-// sums (FP64) to part[cta][2 * npairs].
+// columns, each padded to kp = 8 np columns): each CTA reduces a contiguous
+// row range and writes its partial sums (FP64) to part[cta][2 * npairs], pair
+// p = (i, j), i <= j, numbered row by row over the upper triangle of the
+// m = nblk k real columns.
+//
+// Register-tiled outer products: the padded m_p x m_p matrix is cut into 8 x 8
+// tiles; the upper-triangle tiles (I <= J) are split into four 4 x 4 sub-tiles,
+// one per thread (4 * T (T + 1) / 2 threads for T = m_p / 8 tile columns, at
+// most 312).  Per staged row a thread reads 4 values of S and 4 of each image
+// and does 32 multiply-adds, so the FP64 form runs on the FP64 pipe instead of
+// on shared-memory loads (the former one-pair-per-slot form read 3 values per
+// 2 multiply-adds).  The sub-tile below the diagonal of a diagonal tile is
+// computed and not written.
 template <typename T>
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(320)
     k_gram(int64_t n, int k, int nblk, const T *S0, const T *S1, const T *S2, const T *K0, const T *K1, const T *K2,
            const T *M0, const T *M1, const T *M2, double *part)
 {
     extern __shared__ unsigned char smraw[];
+    const int kp = (k + PW - 1) / PW * PW;
+    const int mp = nblk * kp;
     const int m = nblk * k;
-    const int np = (k + PW - 1) / PW;
     const int npairs = m * (m + 1) / 2;
+    const int tiles = mp / PW;
+    const int ntasks = kGramSub * tiles * (tiles + 1) / 2;
     T *sS = (T *)smraw;
-    T *sK = sS + kGramRows * m;
-    T *sM = sK + kGramRows * m;
-    // this thread's pairs (i <= j)
-    int pi[kMaxPairsPerThread], pj[kMaxPairsPerThread];
-    GramAcc<T> aA[kMaxPairsPerThread], aB[kMaxPairsPerThread];
-    int cnt = 0;
-#pragma unroll
-    for (int u = 0; u < kMaxPairsPerThread; ++u) {
-        // pair p = threadIdx.x + u * blockDim.x -> (i, j), i <= j, row-wise over the upper triangle
-        const int p = threadIdx.x + u * blockDim.x;
-        int i = 0, rem = p < npairs ? p : 0;
-        while (rem >= m - i) {
-            rem -= m - i;
-            ++i;
+    T *sK = sS + kGramRows * mp;
+    T *sM = sK + kGramRows * mp;
+    const bool active = (int)threadIdx.x < ntasks;
+    int i0 = 0, j0 = 0;
+    if (active) {
+        const int tp = threadIdx.x >> 2, sub = threadIdx.x & 3;
+        int I = 0, rem = tp;
+        while (rem >= tiles - I) {
+            rem -= tiles - I;
+            ++I;
         }
-        pi[u] = i;
-        pj[u] = i + rem;
-        aA[u].zero();
-        aB[u].zero();
-        if (p < npairs) cnt = u + 1;
+        i0 = PW * I + kGramSub * (sub >> 1);
+        j0 = PW * (I + rem) + kGramSub * (sub & 1);
     }
+    GramAcc<T> aA[kGramSub][kGramSub], aB[kGramSub][kGramSub];
+#pragma unroll
+    for (int a = 0; a < kGramSub; ++a)
+#pragma unroll
+        for (int b = 0; b < kGramSub; ++b) {
+            aA[a][b].zero();
+            aB[a][b].zero();
+        }
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
     const T *SS[3] = {S0, S1, S2}, *KK[3] = {K0, K1, K2}, *MM[3] = {M0, M1, M2};
     for (int64_t t0 = r0; t0 < r1; t0 += kGramRows) {
         const int rows = (int)((r1 - t0) < (int64_t)kGramRows ? (r1 - t0) : (int64_t)kGramRows);
         __syncthreads();
-        // stage rows: element (r, b, q, c) of each block's panel q
-        const int per_row = nblk * np * PW;
-        for (int e = threadIdx.x; e < rows * per_row; e += blockDim.x) {
-            const int r = e / per_row;
-            int rem = e - r * per_row;
-            const int b = rem / (np * PW);
-            rem -= b * np * PW;
-            const int q = rem / PW, c = rem - q * PW;
-            const int col = q * PW + c;
-            if (col >= k) continue;
+        // stage rows t0 .. t0+rows of every padded column; padding columns read as 0
+        for (int e = threadIdx.x; e < rows * mp; e += blockDim.x) {
+            const int r = e / mp, col = e - r * mp;
+            const int b = col / kp, cc = col - b * kp;
+            const int q = cc / PW, c = cc - q * PW;
             const int64_t off = ((int64_t)q * n + t0 + r) * PW + c;
-            const int j = b * k + col;
-            sS[r * m + j] = SS[b][off];
-            sK[r * m + j] = KK[b][off];
-            sM[r * m + j] = MM[b][off];
+            const bool real = cc < k;
+            sS[r * mp + col] = real ? SS[b][off] : T(0);
+            sK[r * mp + col] = real ? KK[b][off] : T(0);
+            sM[r * mp + col] = real ? MM[b][off] : T(0);
         }
         __syncthreads();
-        for (int r = 0; r < rows; ++r) {
-            const T *s = sS + r * m, *kk = sK + r * m, *mm = sM + r * m;
-            // fully unrolled with a guard: the accumulators stay in registers
+        if (active) {
+            for (int r = 0; r < rows; ++r) {
+                T si[kGramSub], yk[kGramSub], ym[kGramSub];
 #pragma unroll
-            for (int u = 0; u < kMaxPairsPerThread; ++u) {
-                if (u < cnt) {
-                    const T si = s[pi[u]];
-                    aA[u].add(si, kk[pj[u]]);
-                    aB[u].add(si, mm[pj[u]]);
+                for (int a = 0; a < kGramSub; ++a) {
+                    si[a] = sS[r * mp + i0 + a];
+                    yk[a] = sK[r * mp + j0 + a];
+                    ym[a] = sM[r * mp + j0 + a];
                 }
+#pragma unroll
+                for (int a = 0; a < kGramSub; ++a)
+#pragma unroll
+                    for (int b = 0; b < kGramSub; ++b) {
+                        aA[a][b].add(si[a], yk[b]);
+                        aB[a][b].add(si[a], ym[b]);
+                    }
             }
         }
     }
+    if (!active) return;
 #pragma unroll
-    for (int u = 0; u < kMaxPairsPerThread; ++u) {
-        const int p = threadIdx.x + u * blockDim.x;
-        if (p < npairs) {
-            part[(int64_t)blockIdx.x * 2 * npairs + p] = aA[u].get();
-            part[(int64_t)blockIdx.x * 2 * npairs + npairs + p] = aB[u].get();
+    for (int a = 0; a < kGramSub; ++a)
+#pragma unroll
+        for (int b = 0; b < kGramSub; ++b) {
+            const int pi = i0 + a, pj = j0 + b;  // padded columns
+            const int bi = pi / kp, ci = pi - bi * kp, bj = pj / kp, cj = pj - bj * kp;
+            if (ci >= k || cj >= k) continue;
+            const int i = bi * k + ci, j = bj * k + cj;
+            if (i > j) continue;
+            const int p = i * m - i * (i - 1) / 2 + (j - i);
+            part[(int64_t)blockIdx.x * 2 * npairs + p] = aA[a][b].get();
+            part[(int64_t)blockIdx.x * 2 * npairs + npairs + p] = aB[a][b].get();
         }
-    }
 }
 
 // Sum the per-CTA partials in CTA order (deterministic).
@@ -595,13 +617,16 @@ void gram(Ctx &c, int nblk, const Blocks<T> &B, std::vector<double> &GA, std::ve
 {
     const int m = nblk * c.k;
     const int npairs = m * (m + 1) / 2;
-    const size_t smem = (size_t)3 * kGramRows * m * sizeof(T);
+    const int mp = nblk * c.kp;
+    const int tiles = mp / PW;
+    const int threads = (kGramSub * tiles * (tiles + 1) / 2 + 31) / 32 * 32;
+    const size_t smem = (size_t)3 * kGramRows * mp * sizeof(T);
     const int g = c.ngrid;
     c.part.ensure((size_t)g * 2 * npairs);
     c.gram.ensure((size_t)2 * npairs);
     PFG_CUDA(cudaFuncSetAttribute(k_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_gram<T><<<g, kT, smem, c.st>>>(c.n, c.k, nblk, B.X.p, B.W.p, B.P.p, B.KX.p, B.KW.p, B.KP.p, B.MX.p, B.MW.p,
-                                     B.MP.p, c.part.p);
+    k_gram<T><<<g, threads, smem, c.st>>>(c.n, c.k, nblk, B.X.p, B.W.p, B.P.p, B.KX.p, B.KW.p, B.KP.p, B.MX.p,
+                                          B.MW.p, B.MP.p, c.part.p);
     k_reduce_parts<<<grid_for(2 * npairs, 256, 64), 256, 0, c.st>>>(c.part.p, g, 2 * npairs, c.gram.p);
     PFG_CUDA(cudaGetLastError());
     c.launches += 2;
