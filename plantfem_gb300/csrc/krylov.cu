@@ -1394,7 +1394,7 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
 // passes in a row whose correction was rejected, before the mixed solve hands
 // over to FP64 (BiCGSTAB's residual is erratic: it gets more room).
 constexpr int kMixedStallCG = 4, kMixedStallBiCG = 8;
-constexpr int kMixedRejectCG = 2, kMixedRejectBiCG = 3;
+constexpr int kMixedRejectCG = 2, kMixedRejectBiCG = 2;
 
 SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st)
 {
@@ -1473,15 +1473,31 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
             }
         }
         double rel = true_residual(A, b, x, r_.p, st);
-        if (!first && !rejected && !(rel < prev_rel)) {
+        // CG's true residual falls from pass to pass; BiCGSTAB's does not
+        // have to (a pass that raised it can still carry the next one to
+        // convergence), so only a correction that blows it up a
+        // thousandfold is dropped
+        const double growth = cg ? 1.0 : 1.0e3;
+        if (!first && !rejected && !(rel < growth * prev_rel)) {
+            if (cfg.debug != 0)
+                fprintf(stderr, "[pfg] mixed iter %d: correction raised |b-Ax|/|b| %.3e -> %.3e\n", h.iter, prev_rel,
+                        rel);
             PFG_CUDA(cudaMemcpyAsync(x, xb_.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
             rel = true_residual(A, b, x, r_.p, st);
             rejected = true;
+        } else if (!first && rejected && cfg.debug != 0) {
+            fprintf(stderr, "[pfg] mixed iter %d: FP32 pass overflowed (breakdowns %d)\n", h.iter, h.breakdowns);
         }
         prev_rel = rel;
         failures = rejected ? failures + 1 : 0;
+        // A rejected pass restarts from the same state and would fail the same
+        // way; within 100x of the target FP64 finishes in a few iterations.
+        if (rejected && rel < 100.0 * cfg.relative_er) failures = std::max(failures, cg ? kMixedRejectCG : kMixedRejectBiCG);
+        if (cfg.debug != 0 && rejected)
+            fprintf(stderr, "[pfg] mixed iter %d: FP32 correction rejected (|b-Ax|/|b| %.3e)\n", h.iter, rel);
         if (failures >= (cg ? kMixedRejectCG : kMixedRejectBiCG) && rel > cfg.relative_er) {
-            // two FP32 passes in a row made no progress: finish in FP64
+            // FP32 passes in a row made no progress: finish in FP64
+            if (cfg.debug != 0) fprintf(stderr, "[pfg] mixed: hand-over to FP64 after rejected corrections\n");
             res.fallback = 1;
             res.iterations = h.iter;
             res.replacements = h.replacements;
@@ -1495,6 +1511,7 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
             best_rel = rel;
             stall = 0;
         } else if (++stall >= (cg ? kMixedStallCG : kMixedStallBiCG) && rel > cfg.relative_er) {
+            if (cfg.debug != 0) fprintf(stderr, "[pfg] mixed: hand-over to FP64 after stalled residuals\n");
             res.fallback = 1;
             res.iterations = h.iter;
             res.replacements = h.replacements;
