@@ -51,6 +51,11 @@ REF_ITERS_LOGNORMAL100 = 1593
 # 1.008), applied to the 1.1238 GB of the 100^3 launch (the kernel's traffic
 # grows in proportion to the blocks it streams).
 TRAFFIC_CG_SPMV_FP32 = 1.1328e9
+# The same for k_cg_spmv_sym (the upper half); None until captured.
+TRAFFIC_CG_SPMV_SYM = None
+# FP32 copy the headline mixed solve reads: "symmetric" (upper half of the
+# symmetric matrix, half the bytes) or "full".
+STORAGE = "symmetric"
 
 
 def peaks():
@@ -168,10 +173,14 @@ def run_ours(args, ws, rank, local):
     x_ref = torch.tensor(x64_host, dtype=torch.float64, device=dev)
     setup_s = time.perf_counter() - t0
 
-    def solve_once(precision, algorithm="CG", pc="BlockJacobi"):
+    def solve_once(precision, algorithm="CG", pc="BlockJacobi", storage=None):
+        # the mixed solve reads the FP32 upper half of the symmetric matrix
+        # (STORAGE); FP64 is FP64-pipe-bound, where half the bytes gain nothing
         x.zero_()
+        if storage is None:
+            storage = STORAGE if precision == "mixed" else "full"
         return s.solve_device(b, x, algorithm=algorithm, preconditioning=pc, precision=precision,
-                              stop_rule="true_relative")
+                              stop_rule="true_relative", storage=storage)
 
     for _ in range(args.warmup):
         solve_once("mixed")
@@ -205,8 +214,17 @@ def run_ours(args, ws, rank, local):
     ev1.record()
     torch.cuda.synchronize()
     ms_f64 = ev0.elapsed_time(ev1) / f64_steps
+    # the same mixed solve from the full FP32 copy (deterministic to the bit)
+    solve_once("mixed", storage="full")
+    ev0.record()
+    full_infos = [solve_once("mixed", storage="full") for _ in range(f64_steps)]
+    ev1.record()
+    torch.cuda.synchronize()
+    ms_full = ev0.elapsed_time(ev1) / f64_steps
 
-    out_extra = {}
+    out_extra = {"mixed_full_storage": {"ms": round(ms_full, 3), "iterations": full_infos[-1]["iterations"],
+                                        "rel_residual": full_infos[-1]["rel_residual"],
+                                        "speedup_vs_fp64": round(ms_f64 / ms_full, 3)}}
     if not args.skip_variants:
         # where the direction update runs: fused into the SpMV gathers or as a
         # separate streaming pass (auto picks per precision)
@@ -215,7 +233,7 @@ def run_ours(args, ws, rank, local):
                                ("cg_mixed_fused", "mixed", 1), ("cg_mixed_separate", "mixed", 2)):
             x.zero_()
             iv = s.solve_device(b, x, algorithm="CG", preconditioning="BlockJacobi", precision=prec,
-                                stop_rule="true_relative", update_mode=um)
+                                stop_rule="true_relative", update_mode=um, storage="full")
             var[name] = {"ms": round(iv["solve_ms"], 2), "iterations": iv["iterations"], "status": iv["status"]}
         out_extra["update_mode_variants"] = var
     # reference algorithm on the GPU: unpreconditioned BiCGSTAB, reference stop rule
@@ -438,23 +456,27 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
              ms_f64, clk, setup_s, t0, t_pat, t_asm, out_extra):
     import torch
     from plantfem_gb300 import _native, linear_solver_crs
-    # kernel roofline: the dominant kernel of the mixed solve (streaming update
-    # passes, the default) is the FP32 3x3-block SELL SpMV with the p.q
-    # reduction, k_cg_spmv_u<3,float>; each is timed with CUDA events on the
-    # handle's stream over 20 back-to-back launches
+    # kernel roofline: the dominant kernel of the mixed solve is the FP32
+    # product from the upper half of the symmetric matrix with the fused
+    # p.Ap reduction, k_cg_spmv_sym (with the full copy: k_cg_spmv_u<3,float>);
+    # each is timed with CUDA events on the handle's stream over 20
+    # back-to-back launches
     import ctypes as C
     prof = {}
     for kid, name in ((0, "spmv_fp64"), (1, "spmv_fp32"), (2, "cg_spmv_fp32_fused"), (5, "cg_spmv_fp32"),
-                      (6, "cg_spmv_fp64")):
+                      (6, "cg_spmv_fp64"), (7, "spmv_fp32_symmetric"), (8, "cg_spmv_fp32_symmetric")):
         ms, by = C.c_double(), C.c_double()
         _native.check(_native.load().pfg_profile_kernel(s.handle, kid, 20, C.byref(ms), C.byref(by)))
         prof[name] = {"ms": ms.value, "bytes": by.value, "GBs": by.value / (ms.value * 1e-3) / 1e9}
     pk = peaks()
     peak = pk["hbm_gbs"] if pk else 6800.0
-    dom_k = prof["cg_spmv_fp32"]
-    roofline = {"kernel": "k_cg_spmv_u<3,float> (FP32 3x3-block SELL SpMV + p.q)", "bound": "hbm",
+    sym = STORAGE == "symmetric"
+    dom_k = prof["cg_spmv_fp32_symmetric" if sym else "cg_spmv_fp32"]
+    roofline = {"kernel": ("k_cg_spmv_sym (FP32 product from the upper 3x3 blocks of the symmetric matrix + p.Ap)"
+                           if sym else "k_cg_spmv_u<3,float> (FP32 3x3-block SELL SpMV + p.q)"), "bound": "hbm",
                 "achieved": round(dom_k["GBs"], 1), "peak": peak, "unit": "GB/s",
-                "frac": round(dom_k["GBs"] / peak, 4), "traffic": TRAFFIC_CG_SPMV_FP32,
+                "frac": round(dom_k["GBs"] / peak, 4),
+                "traffic": TRAFFIC_CG_SPMV_SYM if sym else TRAFFIC_CG_SPMV_FP32,
                 "bytes_per_launch": dom_k["bytes"], "ms_per_launch": round(dom_k["ms"], 5),
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if pk else "fallback 6800 GB/s"}
 
@@ -470,13 +492,13 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
         xh = torch.zeros(ndof, dtype=torch.float64).pin_memory()
         rpn, cin, valn, rhsn, xn = rp_p.numpy(), ci_p.numpy(), val_p.numpy(), rhs_p.numpy(), xh.numpy()
         xn[:] = 0
-        linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL)  # warm-up: allocations, graphs
+        linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL, storage=STORAGE)  # warm-up: allocations, graphs
         e2e_steps = max(1, min(args.steps, 3))
         t_a = time.perf_counter()
         e2e_infos = []
         for _ in range(e2e_steps):
             xn[:] = 0
-            e2e_infos.append(linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL))
+            e2e_infos.append(linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL, storage=STORAGE))
         t_e2e = (time.perf_counter() - t_a) / e2e_steps
         h2d = rpn.nbytes + cin.nbytes + valn.nbytes + rhsn.nbytes + xn.nbytes
         e2e = {"value": round(ws / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
@@ -515,8 +537,11 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
         "ms_per_step": round(ms_step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 inner / f64 residual", "data": "synthetic (seeded lognormal E, numpy seed 20261203)",
         "config": {"workload": f"lognormal{n}: Cube3D {n}^3 hex8, {ndof} DOF, E~lognormal(ln1e4, 0.5), nu 0.3, "
-                               "z=0 fixed, top traction -1; CG + 3x3 block Jacobi; rel. residual 1e-10",
-                   "l2": f"inputs larger than L2 (FP32 matrix {prof['spmv_fp32']['bytes'] / 1e9:.2f} GB read "
+                               "z=0 fixed, top traction -1; CG + 3x3 block Jacobi; rel. residual 1e-10; "
+                               f"FP32 copy: {STORAGE}",
+                   "l2": f"inputs larger than L2 (FP32 matrix "
+                         f"{prof['spmv_fp32_symmetric' if STORAGE == 'symmetric' else 'spmv_fp32']['bytes'] / 1e9:.2f}"
+                         " GB read "
                          "per SpMV)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "mixed": {"iterations": mixed_info["iterations"], "replacements": mixed_info["replacements"],

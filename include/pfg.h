@@ -49,6 +49,13 @@ extern "C" {
 #define PFG_PREC_FP64 0         /* every operation in FP64 (the plain drop-in) */
 #define PFG_PREC_MIXED 1        /* FP32 inner iterations, FP64 residual replacement */
 
+/* Storage of the FP32 copy the mixed inner iterations read (no reference
+ * counterpart; the reference keeps one FP64 CRS). */
+#define PFG_STORAGE_FULL 0       /* every block: deterministic, works for any matrix */
+#define PFG_STORAGE_SYMMETRIC 1  /* upper half of a symmetric 3x3-block matrix: half the bytes per
+                                    product; checked symmetric (else PFG_E_ARG); the FP32 sums'
+                                    order, hence their last bits, varies from run to run */
+
 #define PFG_PC_NONE 0           /* unpreconditioned, as the reference */
 #define PFG_PC_JACOBI 1         /* point Jacobi (JacobiPreconditionerCRS, FEMSolverClass.f90:2508-2529) */
 #define PFG_PC_BLOCK_JACOBI 2   /* inverse of each 3x3 diagonal node block */
@@ -70,6 +77,7 @@ typedef struct pfg_solve_opts {
     int32_t debug;           /* FEMSolver_%debug: print the residual per graph chunk */
     int32_t update_mode;     /* 0 auto, 1 vector updates fused into the SpMV gathers,
                                 2 separate streaming passes (see krylov.cu) */
+    int32_t storage;         /* mixed: PFG_STORAGE_FULL (default) or PFG_STORAGE_SYMMETRIC */
 } pfg_solve_opts;
 
 typedef struct pfg_info {
@@ -352,8 +360,11 @@ int pfg_batch_abort_flag(pfg_batch *b, volatile int32_t **flag);
  * SpMV, 1 = FP32 block SpMV, 2 = the FP32 CG SpMV with the fused direction
  * update, 3 / 4 = FP64 / FP32 warp-per-row BCRS SpMV, 5 / 6 = the FP32 / FP64
  * CG SpMV with the p.q reduction (the dominant kernels of the mixed and FP64
- * solves with streaming update passes, the default).  Kernels 2, 5 and 6 need
- * a symmetric positive definite (eliminated) matrix. */
+ * solves with streaming update passes, the default), 7 = the FP32 product from
+ * the upper half of a symmetric matrix (PFG_STORAGE_SYMMETRIC), 8 = its CG form
+ * with the fused p.Ap (the dominant kernel of the symmetric-storage mixed CG).
+ * Kernels 2, 5, 6 and 8 need a symmetric positive definite (eliminated)
+ * matrix, 7 a symmetric one. */
 int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, double *ms_per_launch, double *bytes_per_launch);
 
 #ifdef __cplusplus

@@ -22,6 +22,7 @@ ERRORS = {
 
 ALG_BICGSTAB, ALG_CG = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
+STORAGE_FULL, STORAGE_SYMMETRIC = 0, 1
 PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI = 0, 1, 2
 STOP_REFERENCE, STOP_TRUE_RELATIVE = 0, 1
 
@@ -36,7 +37,7 @@ class SolveOpts(C.Structure):
     _fields_ = [("algorithm", C.c_int32), ("precision", C.c_int32), ("precond", C.c_int32),
                 ("stop_rule", C.c_int32), ("itrmax", C.c_int32), ("graph_chunk", C.c_int32),
                 ("er0", C.c_double), ("relative_er", C.c_double), ("reliable_delta", C.c_double),
-                ("debug", C.c_int32), ("update_mode", C.c_int32)]
+                ("debug", C.c_int32), ("update_mode", C.c_int32), ("storage", C.c_int32)]
 
 
 class EigOpts(C.Structure):

@@ -127,6 +127,7 @@ KConfig to_config(const pfg_solve_opts *o)
     c.graph_chunk = o->graph_chunk;
     c.debug = o->debug;
     c.fuse = o->update_mode == 1 ? 1 : (o->update_mode == 2 ? 0 : -1);
+    c.storage = o->storage;
     return c;
 }
 

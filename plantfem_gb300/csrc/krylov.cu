@@ -397,10 +397,10 @@ __global__ void __launch_bounds__(kThreads)
 // x += alpha p_new; r -= alpha q; z = M^-1 r; rho' = r.z; rr = r.r.
 // fin (FP64): beta = rho'/rho, stop test on the recursive residual.
 // fin (FP32): same, or request a residual replacement.
-template <int BS, typename T>
+template <int BS, typename T, int QS = BS>
 __global__ void __launch_bounds__(kThreads)
     k_cg_update(int64_t nb, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *pA, const T *pB,
-                const T *__restrict__ q, const T *__restrict__ dinv, int pc, KState *S, double *pd, float *pf,
+                T *__restrict__ q, const T *__restrict__ dinv, int pc, KState *S, double *pd, float *pf,
                 unsigned *ticket, double tol, double delta, int itrmax)
 {
     if (S->done | S->need_update) return;
@@ -414,8 +414,12 @@ __global__ void __launch_bounds__(kThreads)
         for (int i = 0; i < BS; ++i) {
             const int64_t j = (int64_t)BS * row + i;
             x[j] = fma(alpha, pnew[j], x[j]);
-            rv[i] = fma(-alpha, q[j], r[j]);
+            rv[i] = fma(-alpha, q[(int64_t)QS * row + i], r[j]);
             r[j] = rv[i];
+        }
+        if (QS == 4) {  // the symmetric product's accumulator: cleared for the next product
+#pragma unroll
+            for (int i = 0; i < 4; ++i) q[4 * row + i] = T(0);
         }
         pc_apply<BS, T>(pc, dinv, row, rv, zv);
 #pragma unroll
@@ -893,6 +897,181 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// ------------------------------------------- symmetric storage (FP32 inner)
+// The FP32 inner iterations of a symmetric matrix can read only its upper
+// half: each stored block (i, j), j >= i, is applied as A_ij x_j to row i and,
+// for j > i, as A_ij^T x_i to row j.  The transposed products are scattered
+// with 16-byte vector reductions (red.global.add.v4.f32) into a 4-per-node
+// accumulator that stays in L2; half the matrix bytes for 1 + (upper blocks)
+// reductions per row.  The summation order of a row's contributions is that
+// of the reductions, so FP32 inner results vary in their last bits from run
+// to run (the FP64 residual and the stop test are computed as always).
+__device__ __forceinline__ void red_add_v4(float *a, float x, float y, float z)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(0.f)
+                 : "memory");
+}
+
+// y4 += A x from the upper half U (y4: 4 floats per block row, zero on entry)
+__global__ void __launch_bounds__(kThreads)
+    k_spmv_sym(SellView<float> U, const float *__restrict__ x, float *__restrict__ y4, const KState *S)
+{
+    if (S && (S->done | S->need_update)) return;
+    PFG_SLICE_LOOP(U)
+    {
+        const int64_t row = s * 32 + lane;
+        const bool live = row < U.nb;
+        float xi[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) xi[t] = live ? __ldg(x + 3 * row + t) : 0.f;
+        const int64_t b0 = U.sptr[s];
+        const int w = (int)(U.sptr[s + 1] - b0);
+        const int *cp = U.col + b0 * 32 + lane;
+        const float *vp = U.val + b0 * 32 * 9 + lane;
+        float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll 2
+        for (int k = 0; k < w; ++k) {
+            const int c = ld_stream(cp + (int64_t)k * 32);
+            float a[9];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[e] = ld_stream(vp + ((int64_t)k * 9 + e) * 32);
+            float xj[3];
+#pragma unroll
+            for (int t = 0; t < 3; ++t) xj[t] = __ldg(x + 3 * (int64_t)c + t);
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int t = 0; t < 3; ++t) acc[r] = fmaf(a[3 * r + t], xj[t], acc[r]);
+            if (live && c != row) {
+                float tv[3];
+#pragma unroll
+                for (int t = 0; t < 3; ++t) tv[t] = fmaf(a[t], xi[0], fmaf(a[3 + t], xi[1], a[6 + t] * xi[2]));
+                red_add_v4(y4 + 4 * (int64_t)c, tv[0], tv[1], tv[2]);
+            }
+        }
+        if (live) red_add_v4(y4 + 4 * row, acc[0], acc[1], acc[2]);
+    }
+}
+
+// CG form: q4 += A p from the upper half and <p, A p> in the same pass,
+// fin: alpha = rho / <p, Ap>.  With acc_i = sum over the row's stored blocks
+// (j >= i) of A_ij p_j, symmetry gives <p, Ap> = sum_i (2 p_i.acc_i - p_i^T A_ii p_i),
+// so the reduction does not wait for the scattered transposes.
+__global__ void __launch_bounds__(kThreads)
+    k_cg_spmv_sym(SellView<float> U, const float *__restrict__ p, float *__restrict__ q4, KState *S, double *pd,
+                  float *pf, unsigned *ticket)
+{
+    if (S->done | S->need_update) return;
+    Comp32 dot[1] = {Comp32{0.f, 0.f}};
+    PFG_SLICE_LOOP(U)
+    {
+        const int64_t row = s * 32 + lane;
+        const bool live = row < U.nb;
+        float xi[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) xi[t] = live ? __ldg(p + 3 * row + t) : 0.f;
+        const int64_t b0 = U.sptr[s];
+        const int w = (int)(U.sptr[s + 1] - b0);
+        const int *cp = U.col + b0 * 32 + lane;
+        const float *vp = U.val + b0 * 32 * 9 + lane;
+        float acc[3] = {0.f, 0.f, 0.f}, dg[3] = {0.f, 0.f, 0.f};
+#pragma unroll 2
+        for (int k = 0; k < w; ++k) {
+            const int c = ld_stream(cp + (int64_t)k * 32);
+            float a[9];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[e] = ld_stream(vp + ((int64_t)k * 9 + e) * 32);
+            float xj[3];
+#pragma unroll
+            for (int t = 0; t < 3; ++t) xj[t] = __ldg(p + 3 * (int64_t)c + t);
+            float bx[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) bx[r] = fmaf(a[3 * r], xj[0], fmaf(a[3 * r + 1], xj[1], a[3 * r + 2] * xj[2]));
+#pragma unroll
+            for (int r = 0; r < 3; ++r) acc[r] += bx[r];
+            if (c == row) {  // the diagonal block (and zero padding)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) dg[r] += bx[r];
+            } else if (live) {
+                float tv[3];
+#pragma unroll
+                for (int t = 0; t < 3; ++t) tv[t] = fmaf(a[t], xi[0], fmaf(a[3 + t], xi[1], a[6 + t] * xi[2]));
+                red_add_v4(q4 + 4 * (int64_t)c, tv[0], tv[1], tv[2]);
+            }
+        }
+        if (live) {
+            red_add_v4(q4 + 4 * row, acc[0], acc[1], acc[2]);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                comp_add_prod(dot[0], 2.f * xi[r], acc[r]);
+                comp_add_prod(dot[0], -xi[r], dg[r]);
+            }
+        }
+    }
+    float tot[1];
+    if (grid_total<1>(dot, pd, pf, ticket, tot)) {
+        const double pq = (double)tot[0];
+        if (!(pq > 0.0) || !finite_d(pq)) {
+            S->status = PFG_E_BREAKDOWN;
+            S->done = 1;
+        } else {
+            S->alpha32 = (float)(S->rho32 / tot[0]);
+        }
+    }
+}
+
+// y = y4 (3 per block row), y4 = 0 for the next product, and the dot products
+// the full-storage SpMV kernels fuse, with their scalar updates:
+//   mode 0 (CG):        <a, y>          -> alpha = rho / <p, Ap>
+//   mode 1 (BiCGSTAB):  <a, y>          -> c2 = <r0, y>, alpha = c1 / c2
+//   mode 2 (BiCGSTAB):  <a, y>, <y, y>  -> c3 = <e, v> / <v, v>
+__global__ void __launch_bounds__(kThreads)
+    k_sym_finish(int64_t nb, float *__restrict__ y4, float *__restrict__ y, const float *__restrict__ a, int mode,
+                 KState *S, double *pd, float *pf, unsigned *ticket)
+{
+    if (S->done | S->need_update) return;
+    Comp32 acc[2] = {Comp32{0.f, 0.f}, Comp32{0.f, 0.f}};
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        float4 *q = reinterpret_cast<float4 *>(y4 + 4 * row);
+        const float4 v = *q;
+        *q = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float yv[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            y[3 * row + t] = yv[t];
+            comp_add_prod(acc[0], a[3 * row + t], yv[t]);
+            if (mode == 2) comp_add_prod(acc[1], yv[t], yv[t]);
+        }
+    }
+    float tot[2];
+    if (grid_total<2>(acc, pd, pf, ticket, tot)) {
+        if (mode == 0) {
+            const double pq = (double)tot[0];
+            if (!(pq > 0.0) || !finite_d(pq)) {
+                S->status = PFG_E_BREAKDOWN;
+                S->done = 1;
+            } else {
+                S->alpha32 = (float)(S->rho32 / tot[0]);
+            }
+        } else if (mode == 1) {
+            const double c2 = (double)tot[0];
+            if (c2 == 0.0 || !finite_d(c2)) {
+                bicg_breakdown(S, false);
+            } else {
+                S->c2_32 = tot[0];
+                S->alpha32 = S->c1_32 / tot[0];
+            }
+        } else {
+            const double vv = (double)tot[1];
+            if (vv == 0.0 || !finite_d(vv) || !finite_d((double)tot[0]))
+                bicg_breakdown(S, false);
+            else
+                S->c3_32 = tot[0] / tot[1];
+        }
+    }
+}
+
 // --------------------------------------------------- mixed-precision plumbing
 // x64 += x32, x32 = 0 (fold the FP32 correction into the FP64 solution).
 __global__ void k_fold(int64_t n, double *__restrict__ x64, float *__restrict__ x32)
@@ -1120,8 +1299,8 @@ uint64_t Krylov::graph_key(int kind, const DevMatrix &A, const void *x, const KC
                     u(pA32_.p), u(pB32_.p), u(q32_.p), u(yA32_.p), u(yB32_.p), u(e32_.p), u(v32_.p), u(x32_.p),
                     u(dinv32_.p), u(ph_.p), u(eh_.p), u(ph32_.p), u(eh32_.p), u(partials_.p), u(partials32_.p), u(ticket_.p), u(state_.p),
                     (uint64_t)cfg.precond, (uint64_t)cfg.stop_rule, (uint64_t)cfg.graph_chunk, (uint64_t)cfg.itrmax,
-                    (uint64_t)cfg.fuse,
-                    d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta)});
+                    (uint64_t)cfg.fuse, (uint64_t)cfg.storage, u(y4_.p), u(A.sptr_u.p), u(A.scol_u.p),
+                    u(A.s32_u.p), d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta)});
 }
 
 // One chunk of CG iterations.  fuse: p = z + beta p formed inside the SpMV
@@ -1195,6 +1374,55 @@ static int bicg_chunk(const SellView<T> &A, bool fuse, int chunk, int64_t nb, T 
     return (fuse ? 3 : 5) * chunk;
 }
 
+// One chunk of FP32 CG iterations with the symmetric (upper-half) matrix:
+// dir, product into q4 with <p, Ap> and alpha, update (reads and clears q4).
+static int cg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *x, float *r, float *z, float *p,
+                        float *q4, const float *dinv, int pc, KState *S, double *pd, float *pf, unsigned *tk,
+                        double tol, double delta, int itrmax, cudaStream_t st)
+{
+    const int64_t n = nb * 3;
+    const int gd = resident_grid(k_cg_dir<float>, (n + 31) / 32);
+    const int gs = resident_grid(k_cg_spmv_sym, U.ns);
+    const int gu = resident_grid(k_cg_update<3, float, 4>, (nb + 31) / 32);
+    for (int it = 0; it < chunk; ++it) {
+        k_cg_dir<float><<<gd, kThreads, 0, st>>>(n, z, p, S);
+        k_cg_spmv_sym<<<gs, kThreads, 0, st>>>(U, p, q4, S, pd, pf, tk);
+        k_cg_update<3, float, 4><<<gu, kThreads, 0, st>>>(nb, x, r, z, p, p, q4, dinv, pc, S, pd, pf, tk, tol,
+                                                          delta, itrmax);
+    }
+    PFG_CUDA(cudaGetLastError());
+    return 3 * chunk;
+}
+
+// One chunk of FP32 BiCGSTAB iterations with the symmetric matrix (the
+// separate-pass structure of bicg_chunk, each product through y4 + finish).
+static int bicg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *x, float *r, float *r0, float *p,
+                          float *y, float *e, float *v, float *ph, float *eh, float *y4, const float *dinv, int pc,
+                          KState *S, double *pd, float *pf, unsigned *tk, double er0, double tol, double delta,
+                          int itrmax, cudaStream_t st)
+{
+    const int64_t nvec = (nb * 3 + 31) / 32;
+    float *phat = pc != PFG_PC_NONE ? ph : p;
+    float *ehat = pc != PFG_PC_NONE ? eh : e;
+    const int gd = resident_grid(k_bicg_dir<3, float>, (nb + 31) / 32);
+    const int ge = resident_grid(k_bicg_e<3, float>, (nb + 31) / 32);
+    const int gs = resident_grid(k_spmv_sym, U.ns);
+    const int gf = resident_grid(k_sym_finish, (nb + 31) / 32);
+    const int g3 = resident_grid(k_bicg_update<3, float>, nvec);
+    for (int it = 0; it < chunk; ++it) {
+        k_bicg_dir<3, float><<<gd, kThreads, 0, st>>>(nb, r, p, y, ph, dinv, pc, S);
+        k_spmv_sym<<<gs, kThreads, 0, st>>>(U, phat, y4, S);
+        k_sym_finish<<<gf, kThreads, 0, st>>>(nb, y4, y, r0, 1, S, pd, pf, tk);
+        k_bicg_e<3, float><<<ge, kThreads, 0, st>>>(nb, r, y, e, eh, dinv, pc, S);
+        k_spmv_sym<<<gs, kThreads, 0, st>>>(U, ehat, y4, S);
+        k_sym_finish<<<gf, kThreads, 0, st>>>(nb, y4, v, e, 2, S, pd, pf, tk);
+        k_bicg_update<3, float><<<g3, kThreads, 0, st>>>(nb, x, r, r0, phat, phat, e, ehat, v, S, pd, pf, tk,
+                                                         PFG_STOP_TRUE_RELATIVE, er0, tol, delta, itrmax);
+    }
+    PFG_CUDA(cudaGetLastError());
+    return 7 * chunk;
+}
+
 SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfig &cfg_in, cudaStream_t st)
 {
     KConfig cfg = cfg_in;
@@ -1205,6 +1433,9 @@ SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfi
     if (cfg.itrmax <= 0) cfg.itrmax = 100000;
     if (cfg.graph_chunk <= 0) cfg.graph_chunk = 32;
     if (cfg.precision == PFG_PREC_MIXED) cfg.stop_rule = PFG_STOP_TRUE_RELATIVE;
+    PFG_CHECK(cfg.storage == PFG_STORAGE_FULL || cfg.storage == PFG_STORAGE_SYMMETRIC, PFG_E_ARG, "unknown storage");
+    // the symmetric copy serves the FP32 inner iterations of 3x3-block systems
+    if (cfg.precision != PFG_PREC_MIXED || A.bs != 3) cfg.storage = PFG_STORAGE_FULL;
     if (cfg.reliable_delta <= 0.0 || cfg.reliable_delta >= 1.0) cfg.reliable_delta = 0.1;
     // update_mode 0 (auto): separate streaming passes.  Measured on GB300 at
     // 3.09M DOF: FP64 CG 894 ms separate vs 1165 ms fused (the fused gather
@@ -1408,6 +1639,13 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
     const int64_t n = A.ndof();
     const int g = row_grid(A.nb);
     const int gv = grid_for(n, 256, sm_count() * 8);
+    const bool sym = cfg.storage == PFG_STORAGE_SYMMETRIC;
+    if (sym) {
+        // upper half (checked symmetric) and its zeroed 4-per-row accumulator
+        build_sell_upper(A, st);
+        y4_.ensure((size_t)A.nb * 4);
+        PFG_CUDA(cudaMemsetAsync(y4_.p, 0, (size_t)A.nb * 4 * sizeof(float), st));
+    }
     const uint64_t key = graph_key(cg ? 3 : 4, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -1416,7 +1654,16 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
         auto body = [&]() {
             const bool fz = cfg.fuse != 0;
             const int ch = cfg.graph_chunk;
-            if (cg)
+            if (sym && cg)
+                nk = cg_chunk_sym(sell_upper(A), ch, A.nb, x32_.p, r32_.p, z32_.p, pA32_.p, y4_.p, dinv32_.p,
+                                  cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
+                                  cfg.reliable_delta, cfg.itrmax, st);
+            else if (sym)
+                nk = bicg_chunk_sym(sell_upper(A), ch, A.nb, x32_.p, r32_.p, r032_.p, pA32_.p, yA32_.p, e32_.p,
+                                    v32_.p, ph32_.p, eh32_.p, y4_.p, dinv32_.p, cfg.precond, state_.p, partials_.p,
+                                    partials32_.p, ticket_.p, cfg.er0, cfg.relative_er, cfg.reliable_delta,
+                                    cfg.itrmax, st);
+            else if (cg)
                 nk = A.bs == 3 ? cg_chunk<3, float>(A.sell<float>(), fz, ch, A.nb, x32_.p, r32_.p, z32_.p, pA32_.p,
                                                     pB32_.p, q32_.p, dinv32_.p, cfg.precond, state_.p, partials_.p,
                                                     partials32_.p, ticket_.p, cfg.relative_er, cfg.reliable_delta,
@@ -1610,7 +1857,8 @@ __global__ void k_fill(double *a, int64_t n, double v)
 
 void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
 {
-    PFG_CHECK(kernel >= 0 && kernel <= 6 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel >= 0 && kernel <= 8 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel < 7 || A.bs == 3, PFG_E_UNSUPPORTED, "the symmetric product is built for 3x3 blocks");
     const int64_t n = A.ndof();
     const double bs2 = (double)(A.bs * A.bs);
     // algorithmic bytes: values and block columns once, row pointers (int64)
@@ -1618,7 +1866,12 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
     const double idx = (double)A.nnzb * 4.0 + (double)(A.nb + 1) * 8.0;
     const bool f64 = kernel == 0 || kernel == 3 || kernel == 6;
     if (kernel == 4 && !A.v32_valid) make_v32(A, st);
-    if (kernel <= 2 || kernel >= 5) build_sell(A, f64, !f64, st);
+    if (kernel <= 2 || kernel == 5 || kernel == 6) build_sell(A, f64, !f64, st);
+    if (kernel >= 7) {
+        build_sell_upper(A, st);
+        y4_.ensure((size_t)A.nb * 4);
+        PFG_CUDA(cudaMemsetAsync(y4_.p, 0, (size_t)A.nb * 4 * sizeof(float), st));
+    }
     const int gv = grid_for(n, 256, sm_count() * 8);
     const int gb = row_grid(A.nb);
     DevBuf<double> x64, y64;
@@ -1674,6 +1927,14 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
                 k_cg_spmv_u<1, double><<<g6, kThreads, 0, st>>>(A.sell<double>(), x64.p, y64.p, state_.p, partials_.p,
                                                                 partials32_.p, ticket_.p);
             break;
+        case 7:
+            k_spmv_sym<<<resident_grid(k_spmv_sym, A.ns_u), kThreads, 0, st>>>(sell_upper(A), x32.p, y4_.p,
+                                                                              nullptr);
+            break;
+        case 8:
+            k_cg_spmv_sym<<<resident_grid(k_cg_spmv_sym, A.ns_u), kThreads, 0, st>>>(
+                sell_upper(A), x32.p, y4_.p, state_.p, partials_.p, partials32_.p, ticket_.p);
+            break;
         case 3:
             if (A.bs == 3) k_spmv<3, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
             else k_spmv<1, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
@@ -1693,6 +1954,9 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
         y32.alloc((size_t)n);
         k_fill<<<gv, 256, 0, st>>>(x32.p, n, 1.0f);
         bytes = (double)A.nnzb * bs2 * 4.0 + idx + 2.0 * (double)n * 4.0;
+        if (kernel >= 7)  // the upper half: (nnzb + nb) / 2 blocks of a symmetric pattern
+            bytes = (double)(A.nnzb + A.nb) / 2.0 * (bs2 * 4.0 + 4.0) + (double)(A.nb + 1) * 8.0 +
+                    2.0 * (double)n * 4.0;
         if (kernel == 2) {
             p32.alloc((size_t)n);
             q32.alloc((size_t)n);
@@ -1715,7 +1979,7 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ms = (double)t / reps;
-    if (kernel == 2 || kernel >= 5) {
+    if (kernel == 2 || kernel == 5 || kernel == 6 || kernel == 8) {
         KState h;
         read_state(h, st);
         PFG_CHECK(!h.done, PFG_E_BREAKDOWN, "profiled CG SpMV hit p.Ap <= 0 (matrix not positive definite)");

@@ -38,6 +38,7 @@ struct KConfig {
     int graph_chunk;
     int debug;
     int fuse;  // 1: vector updates ride in the SpMV gathers, 0: separate streaming passes
+    int storage = 0;  // mixed: 0 full FP32 copy, 1 upper half of a symmetric matrix (PFG_STORAGE_*)
 };
 
 struct SolveResult {
@@ -68,15 +69,23 @@ struct DevMatrix {
     DevBuf<double> s64;
     DevBuf<float> s32;
     bool sell_pattern = false, s64_valid = false, s32_valid = false;
+    // Upper half (block column >= block row) of a symmetric 3x3-block matrix,
+    // sliced like the full copy, FP32 values: the symmetric-storage inner
+    // iterations read half the matrix bytes (sell.cu, krylov.cu k_spmv_sym).
+    int64_t ns_u = 0;
+    DevBuf<int64_t> sptr_u;
+    DevBuf<int> scol_u;
+    DevBuf<float> s32_u;
+    bool sell_u_pattern = false, s32_u_valid = false;
 
     int64_t ndof() const { return nb * bs; }
     // v64 changed: every derived copy is stale
-    void values_changed() { v32_valid = s64_valid = s32_valid = false; }
+    void values_changed() { v32_valid = s64_valid = s32_valid = s32_u_valid = false; }
     // rp/col changed too
     void pattern_changed()
     {
         values_changed();
-        sell_pattern = false;
+        sell_pattern = sell_u_pattern = false;
     }
     template <typename T>
     BsrView<T> view() const;
@@ -95,6 +104,15 @@ inline SellView<float> DevMatrix::sell<float>() const { return SellView<float>{n
 // Build (or refresh) the sliced-ELL copy: pattern once, FP64 and/or FP32
 // values when stale.  Implemented in sell.cu.
 void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st);
+
+// Build (or refresh) the FP32 upper-half sliced copy of a 3x3-block matrix;
+// checks once per value change that the matrix is symmetric (blockwise, to
+// 1e-9 relative) and throws PFG_E_ARG if it is not.  Implemented in sell.cu.
+void build_sell_upper(DevMatrix &A, cudaStream_t st);
+inline SellView<float> sell_upper(const DevMatrix &A)
+{
+    return SellView<float>{A.nb, A.ns_u, A.sptr_u.p, A.scol_u.p, A.s32_u.p};
+}
 
 // Inverse of every diagonal block (PFG_PC_BLOCK_JACOBI) or diagonal entry
 // (PFG_PC_JACOBI) of A into d64 (and d32 unless null), BS*BS values per block
@@ -136,6 +154,7 @@ class Krylov {
     // FP64 work vectors
     DevBuf<double> r_, r0_, z_, pA_, pB_, q_, yA_, yB_, e_, v_, dinv_, ph_, eh_;
     DevBuf<double> xb_;  // mixed: x before the fold of an FP32 correction
+    DevBuf<float> y4_;   // symmetric storage: 4-per-row product accumulator
     // FP32 work vectors
     DevBuf<float> r32_, r032_, z32_, pA32_, pB32_, q32_, yA32_, yB32_, e32_, v32_, x32_, dinv32_, ph32_, eh32_;
     DevBuf<double> partials_;

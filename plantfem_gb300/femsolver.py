@@ -179,7 +179,8 @@ class FEMSolver:
                                   0.0 if FixValue is None else float(FixValue)))
 
     # ------------------------------------------------------------- solving
-    def _opts(self, algorithm, precision, preconditioning, stop_rule, update_mode=0, reliable_delta=None):
+    def _opts(self, algorithm, precision, preconditioning, stop_rule, update_mode=0, reliable_delta=None,
+              storage="full"):
         alg = {"BiCGSTAB": N.ALG_BICGSTAB, "CG": N.ALG_CG}[algorithm or "BiCGSTAB"]
         prec = {"fp64": N.PREC_FP64, "FP64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
         pc = {None: N.PC_NONE, "None": N.PC_NONE, "PointJacobi": N.PC_JACOBI, "Jacobi": N.PC_JACOBI,
@@ -190,13 +191,14 @@ class FEMSolver:
         um = {0: 0, "auto": 0, 1: 1, "fused": 1, 2: 2, "separate": 2}[update_mode]
         o = N.default_opts(algorithm=alg, precision=prec, precond=pc, stop_rule=sr, itrmax=int(self.itrmax),
                            er0=float(self.er0), relative_er=float(self.relative_er), debug=int(bool(self.debug)),
-                           update_mode=um)
+                           update_mode=um, storage={"full": N.STORAGE_FULL, "symmetric": N.STORAGE_SYMMETRIC}[storage])
         if reliable_delta is not None:
             o.reliable_delta = float(reliable_delta)
         return o
 
     def solve(self, algorithm: str | None = None, preconditioning: str | None = None, x0=None,
-              precision: str = "fp64", stop_rule: str | None = None, update_mode=0) -> np.ndarray:
+              precision: str = "fp64", stop_rule: str | None = None, update_mode=0,
+              storage: str = "full") -> np.ndarray:
         """x = FEMSolver_%solve([algorithm], [preconditioning], [x0]) (FEMSolverClass.f90:1697-1825).
 
         Defaults reproduce the reference: unpreconditioned BiCGSTAB in FP64 with
@@ -204,7 +206,7 @@ class FEMSolver:
         ``precision="mixed"`` select the GB300 forms.  Breakdown raises
         (the reference stops); itrmax is reported in ``last_info``.
         """
-        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode)
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, storage=storage)
         n = self.ndof()
         x = np.zeros(n)
         xi = None if x0 is None else _f64(x0)
@@ -288,10 +290,10 @@ class FEMSolver:
         return lam, (None if X is None else X.T)
 
     def solve_device(self, b, x, algorithm="CG", preconditioning="BlockJacobi", precision="mixed",
-                     stop_rule=None, stream=None, update_mode=0, reliable_delta=None):
+                     stop_rule=None, stream=None, update_mode=0, reliable_delta=None, storage="full"):
         """Solve with the already-eliminated matrix on device tensors b -> x
         (x holds x0).  ``b`` and ``x`` are float64 CUDA tensors."""
-        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, reliable_delta)
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, reliable_delta, storage)
         info = N.Info()
         if stream is None:
             _torch_sync()  # the library works on its own stream: order after the caller's writes
@@ -332,13 +334,14 @@ def crs_spmv_real32(val, row_ptr, col_idx, old_vector, new_vector):
 
 
 def linear_solver_crs(row_ptr, col_idx, val, rhs, x, algorithm="CG", precision="mixed",
-                      preconditioning="BlockJacobi", relative_er=1e-10, itrmax=100000, stop_rule=None):
+                      preconditioning="BlockJacobi", relative_er=1e-10, itrmax=100000, stop_rule=None,
+                      storage="full"):
     """The LinearSolver(row_ptr, col_idx, val, rhs, x) plug-in of FEMSolver_%solve
     (FEMSolverClass.f90:1632-1662) on the GPU; x is updated in place."""
     lib = N.load()
     s = FEMSolver.__new__(FEMSolver)
     s.itrmax, s.er0, s.relative_er, s.debug = itrmax, 1e-10, relative_er, False
-    opts = FEMSolver._opts(s, algorithm, precision, preconditioning, stop_rule)
+    opts = FEMSolver._opts(s, algorithm, precision, preconditioning, stop_rule, storage=storage)
     rp, ci, v, b = _i64(row_ptr), _i32(col_idx), _f64(val), _f64(rhs)
     assert x.dtype == np.float64 and x.flags["C_CONTIGUOUS"]
     info = N.Info()
