@@ -957,7 +957,9 @@ __global__ void __launch_bounds__(kThreads)
 // fin: alpha = rho / <p, Ap>.  With acc_i = sum over the row's stored blocks
 // (j >= i) of A_ij p_j, symmetry gives <p, Ap> = sum_i (2 p_i.acc_i - p_i^T A_ii p_i),
 // so the reduction does not wait for the scattered transposes.
-__global__ void __launch_bounds__(kThreads)
+// 5 CTAs per SM (<= 51 registers) with the slot loop not unrolled: measured
+// 104 us per launch at 3.09M DOF vs 129 us at the default 58 registers.
+__global__ void __launch_bounds__(kThreads, 5)
     k_cg_spmv_sym(SellView<float> U, const float *__restrict__ p, float *__restrict__ q4, KState *S, double *pd,
                   float *pf, unsigned *ticket)
 {
@@ -975,7 +977,7 @@ __global__ void __launch_bounds__(kThreads)
         const int *cp = U.col + b0 * 32 + lane;
         const float *vp = U.val + b0 * 32 * 9 + lane;
         float acc[3] = {0.f, 0.f, 0.f}, dg[3] = {0.f, 0.f, 0.f};
-#pragma unroll 2
+#pragma unroll 1
         for (int k = 0; k < w; ++k) {
             const int c = ld_stream(cp + (int64_t)k * 32);
             float a[9];
