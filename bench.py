@@ -138,7 +138,8 @@ def max_over_ranks(v, ws):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -651,7 +652,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT, help="elements per cube edge (100 = the benchmark)")
+    ap.add_argument("--n", "--cube-n", dest="n", type=int, default=N_DEFAULT,
+                    help="elements per cube edge (100 = the benchmark); --cube-n under torchrun, whose own "
+                         "options take every prefix of --n")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-bicgstab", action="store_true")

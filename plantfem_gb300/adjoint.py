@@ -23,7 +23,8 @@ class ElasticOperator:
     """Mesh, Poisson ratios, load and fixed DOFs of one elasticity problem."""
 
     def __init__(self, domain, nu, rhs, fix_ids, precision: str = "fp64", relative_er: float = 1e-12,
-                 recompute_u: bool = False, algorithm: str = "CG", preconditioning: str = "BlockJacobi"):
+                 recompute_u: bool = False, algorithm: str = "CG", preconditioning: str = "BlockJacobi",
+                 storage: str = "symmetric"):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.s = FEMSolver()
         self.s.setDomain(domain)
@@ -41,6 +42,8 @@ class ElasticOperator:
         self.recompute_u = recompute_u
         self.algorithm = algorithm
         self.preconditioning = preconditioning
+        # K(E) is symmetric: the mixed inner iterations read its upper half
+        self.storage = storage
         self._token = 0      # increases at every assembly
         self._held = None    # token of the matrix the handle holds
 
@@ -56,7 +59,7 @@ class ElasticOperator:
     def _solve(self, b: torch.Tensor) -> torch.Tensor:
         x = torch.zeros(self.n, dtype=torch.float64, device=self.dev)
         self.s.solve_device(b, x, algorithm=self.algorithm, preconditioning=self.preconditioning,
-                            precision=self.precision, stop_rule="true_relative")
+                            precision=self.precision, stop_rule="true_relative", storage=self.storage)
         self.last_info = self.s.last_info
         return x
 
