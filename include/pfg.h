@@ -286,6 +286,37 @@ int pfg_dev_set_rhs(pfg_solver *h, int64_t n, const double *d_rhs, void *stream)
 int pfg_dev_adjoint_grad_E(pfg_solver *h, const double *d_u, const double *d_lambda, int64_t n_prop,
                            const double *d_nu, double *d_grad, void *stream);
 
+/* ------------------------------------------------ Newmark-beta time stepping */
+/* SeismicAnalysis_%LinearReyleighNewmark (SeismicAnalysisClass.f90:1255-1436;
+ * formulas getNewmarkBetaMatrix/Vector and updateVelocity/AccelNewmarkBeta,
+ * :1464-1535) on the GPU.  The reference rebuilds and re-solves the element
+ * matrices every step; here the stiffness kept as "A" and the consistent mass
+ * kept as "B" (pfg_keep_this_matrix_as) are combined once into
+ *   A_eff = M / (b dt^2) + g / (b dt) C + K,   C = alpha M + beta K (Rayleigh),
+ * which replaces the handle's working matrix, with the handle's fixes
+ * eliminated (prescribed displacements held at every step).  Each step forms
+ *   R = M a_ext + M (u/(b dt^2) + v/(b dt) + (1/(2b) - 1) a)
+ *     + C (g/(b dt) u + (g/b - 1) v + dt (g/(2b) - 1) a)
+ * with two SpMVs, solves A_eff u' = R from u (warm start) and updates v, a.
+ * u, v, a start at zero (fixed values in u). */
+typedef struct pfg_newmark_params {
+    double dt;               /* SeismicAnalysis_%dt, default 1 */
+    double newmark_beta;     /* default 0.25 */
+    double newmark_gamma;    /* default 0.5 */
+    double rayleigh_alpha;   /* SeismicAnalysis_%alpha, default 0.524 */
+    double rayleigh_beta;    /* SeismicAnalysis_%beta, default 0.00129 */
+} pfg_newmark_params;
+
+void pfg_newmark_params_default(pfg_newmark_params *p);
+int pfg_newmark_setup(pfg_solver *h, const pfg_newmark_params *p);
+/* Initial state (host arrays of 3 nn, each may be NULL to keep it). */
+int pfg_newmark_set_state(pfg_solver *h, int64_t n, const double *u, const double *v, const double *a);
+/* One time step: a_ext (external acceleration, F = M a_ext; NULL = 0); opts
+ * NULL: CG + block Jacobi to the true relative residual 1e-10 (A_eff is
+ * symmetric positive definite).  u_out, v_out, a_out: NULL or host arrays. */
+int pfg_newmark_step(pfg_solver *h, const pfg_solve_opts *opts, int64_t n, const double *a_ext, double *u_out,
+                     double *v_out, double *a_out, pfg_info *info);
+
 /* ------------------------------------------------------------ batched solves */
 /* No single reference call: plantFEM solves one organ mesh per FEMSolver_
  * object and calls FEMSolver_%solve on each in turn (FEMSolverClass.f90:1707

@@ -6,12 +6,14 @@ this package is the thin Python side of that ABI:
 * :class:`FEMDomain` -- structured hex8 meshes (``Cube3D``), selection;
 * :class:`FEMSolver` -- plantFEM's ``FEMSolver_`` call surface;
 * :class:`FEMSolverBatch` -- many FEMSolver systems in one persistent launch;
+* :class:`SeismicAnalysis` -- linear Newmark-beta time stepping with Rayleigh damping;
 * :mod:`problems` -- the benchmark problems (meshes, loads, boundary conditions);
 * :func:`build` -- compile the library in-tree.
 """
 from .femdomain import FEMDomain
 from .femsolver import FEMSolver, crs_spmv_real32, crs_spmv_real64, linear_solver_crs
 from .batch import FEMSolverBatch
+from .seismic import SeismicAnalysis
 from . import problems
 
 
@@ -20,5 +22,5 @@ def build(verbose: bool = False) -> str:
     return _b(verbose=verbose)
 
 
-__all__ = ["FEMDomain", "FEMSolver", "FEMSolverBatch", "crs_spmv_real64", "crs_spmv_real32", "linear_solver_crs", "problems",
+__all__ = ["FEMDomain", "FEMSolver", "FEMSolverBatch", "SeismicAnalysis", "crs_spmv_real64", "crs_spmv_real32", "linear_solver_crs", "problems",
            "build"]

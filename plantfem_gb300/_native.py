@@ -49,6 +49,11 @@ class EigOpts(C.Structure):
 EIG_STOP_REFERENCE, EIG_STOP_RESIDUAL = 0, 1
 
 
+class NewmarkParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("newmark_beta", C.c_double), ("newmark_gamma", C.c_double),
+                ("rayleigh_alpha", C.c_double), ("rayleigh_beta", C.c_double)]
+
+
 class BatchConfig(C.Structure):
     _fields_ = [("threads", C.c_int32), ("cluster", C.c_int32), ("team_fraction", C.c_double)]
 
@@ -123,6 +128,10 @@ SIGNATURES = {
     "pfg_dev_assemble_stiffness": (C.c_int, [_P, _i64, _P, _P, _P]),
     "pfg_dev_set_rhs": (C.c_int, [_P, _i64, _P, _P]),
     "pfg_dev_adjoint_grad_E": (C.c_int, [_P, _P, _P, _i64, _P, _P, _P]),
+    "pfg_newmark_params_default": (None, [C.POINTER(NewmarkParams)]),
+    "pfg_newmark_setup": (C.c_int, [_P, C.POINTER(NewmarkParams)]),
+    "pfg_newmark_set_state": (C.c_int, [_P, _i64, _P, _P, _P]),
+    "pfg_newmark_step": (C.c_int, [_P, C.POINTER(SolveOpts), _i64, _P, _P, _P, _P, C.POINTER(Info)]),
     "pfg_batch_create": (C.c_int, [C.POINTER(_P)]),
     "pfg_batch_destroy": (C.c_int, [_P]),
     "pfg_batch_set": (C.c_int, [_P, _i64, _P]),

@@ -49,6 +49,12 @@ struct pfg_solver {
     // keepThisMatrixAs stack (FEMSolverClass.f90:1544-1604), at most 10 names
     std::vector<std::pair<std::string, DevMatrix>> stack;
     std::vector<int> fix_eig_ids;  // 1-based, unique, sorted (fix_eig, :1607-1628)
+    // linear Newmark-beta time stepping (pfg_newmark_*): parameters and state
+    struct Newmark {
+        bool ready = false;
+        double dt = 0, beta = 0, gamma = 0, ray_alpha = 0, ray_beta = 0;
+        DevBuf<double> u, v, a, base, wM, wK, rhs, tmp, x;
+    } nm;
 
     int64_t ndof() const { return K.ndof(); }
 };
@@ -901,3 +907,183 @@ BatchSource batch_bind(pfg_solver *h)
 }
 
 }  // namespace pfg
+
+// ---------------------------------------------------- Newmark-beta time stepping
+namespace {
+
+// out = cM * M + cK * K over the value arrays of two matrices of one pattern
+__global__ void k_combine_values(int64_t len, double cM, const double *__restrict__ M, double cK,
+                                 const double *__restrict__ K, double *__restrict__ out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = fma(cM, M[i], cK * K[i]);
+}
+
+// weights of the Newmark right-hand side R = M wM + K wK (the C = alpha M + beta K
+// terms folded into both; a_ext: external acceleration, F = M a_ext)
+__global__ void k_newmark_weights(int64_t n, const double *__restrict__ a_ext, const double *__restrict__ u,
+                                  const double *__restrict__ v, const double *__restrict__ a, double mu, double mv,
+                                  double ma, double ku, double kv, double ka, double *__restrict__ wM,
+                                  double *__restrict__ wK)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ae = a_ext ? a_ext[i] : 0.0;
+        wM[i] = ae + mu * u[i] + mv * v[i] + ma * a[i];
+        wK[i] = ku * u[i] + kv * v[i] + ka * a[i];
+    }
+}
+
+// rhs = R + base on free rows (base = -A_eff[:, fixed] u_fixed), prescribed value on fixed rows
+__global__ void k_newmark_rhs(int64_t n, double *__restrict__ rhs, const double *__restrict__ tmp,
+                              const double *__restrict__ base, const uint8_t *__restrict__ fixed)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        rhs[i] = (fixed && fixed[i]) ? base[i] : rhs[i] + tmp[i] + base[i];
+}
+
+// updateVelocity / updateAccelNewmarkBeta (SeismicAnalysisClass.f90:1501-1535), then u = u'
+__global__ void k_newmark_update(int64_t n, const double *__restrict__ un, double *__restrict__ u,
+                                 double *__restrict__ v, double *__restrict__ a, double beta, double gamma, double dt)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double du = un[i] - u[i];
+        const double vn = gamma / (beta * dt) * du + (1.0 - gamma / beta) * v[i] + dt * (1.0 - gamma / (2.0 * beta)) * a[i];
+        const double an = du / (beta * dt * dt) - v[i] / (beta * dt) + (1.0 - 1.0 / (2.0 * beta)) * a[i];
+        u[i] = un[i];
+        v[i] = vn;
+        a[i] = an;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void pfg_newmark_params_default(pfg_newmark_params *p)
+{
+    if (!p) return;
+    // SeismicAnalysis_ defaults (SeismicAnalysisClass.f90:98-109)
+    p->dt = 1.0;
+    p->newmark_beta = 0.25;
+    p->newmark_gamma = 0.5;
+    p->rayleigh_alpha = 0.524;
+    p->rayleigh_beta = 0.00129;
+}
+
+int pfg_newmark_setup(pfg_solver *h, const pfg_newmark_params *p)
+{
+    return guard([&] {
+        need(h && p, PFG_E_ARG, "NULL argument");
+        need(p->dt > 0.0 && p->newmark_beta > 0.0 && p->newmark_gamma > 0.0, PFG_E_ARG,
+             "Newmark: dt, beta and gamma must be positive");
+        std::lock_guard<std::mutex> lk(h->mu);
+        flush_pending(h);
+        DevMatrix *Kp = find_slot(h, "A"), *Mp = find_slot(h, "B");
+        need(Kp && Mp, PFG_E_STATE, "Newmark: keep the stiffness as \"A\" and the mass as \"B\" first");
+        need(Kp->bs == Mp->bs && Kp->nb == Mp->nb && Kp->nnzb == Mp->nnzb, PFG_E_ARG,
+             "Newmark: stiffness and mass must share one CRS pattern");
+        const double b = p->newmark_beta, g = p->newmark_gamma, dt = p->dt;
+        // getNewmarkBetaMatrix (SeismicAnalysisClass.f90:1464-1476) with C = alpha M + beta K
+        const double cM = 1.0 / (b * dt * dt) + g / (b * dt) * p->rayleigh_alpha;
+        const double cK = 1.0 + g / (b * dt) * p->rayleigh_beta;
+        copy_matrix(*Kp, h->K, h->st);
+        const int64_t len = Kp->nnzb * Kp->bs * Kp->bs;
+        k_combine_values<<<grid_for(len, 256, 152 * 16), 256, 0, h->st>>>(len, cM, Mp->v64.p, cK, Kp->v64.p,
+                                                                          h->K.v64.p);
+        PFG_CUDA(cudaGetLastError());
+        h->K.values_changed();
+        h->have_crs = true;
+        const int64_t n = h->K.ndof();
+        auto &nm = h->nm;
+        for (DevBuf<double> *v : {&nm.u, &nm.v, &nm.a, &nm.base, &nm.wM, &nm.wK, &nm.rhs, &nm.tmp, &nm.x})
+            v->resize((size_t)n);
+        for (DevBuf<double> *v : {&nm.u, &nm.v, &nm.a, &nm.base})
+            PFG_CUDA(cudaMemsetAsync(v->p, 0, n * sizeof(double), h->st));
+        // symmetric elimination of the fixed DOFs (LinearSolver_%fix,
+        // LinearSolverClass.f90:266-290); on a zero right-hand side it leaves
+        // base = -A_eff[:, fixed] u_fixed on free rows and u_fixed on fixed rows
+        if (h->have_fix) {
+            h->fixed_d.ensure((size_t)n);
+            h->fixval_d.ensure((size_t)n);
+            PFG_CUDA(cudaMemcpyAsync(h->fixed_d.p, h->fixed_h.data(), n, cudaMemcpyHostToDevice, h->st));
+            PFG_CUDA(cudaMemcpyAsync(h->fixval_d.p, h->fixval_h.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+                                     h->st));
+            apply_dirichlet(h->K, nm.base.p, h->fixed_d.p, h->fixval_d.p, h->st);
+            restore_fixed(n, nm.u.p, h->fixed_d.p, h->fixval_d.p, h->st);
+        }
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        nm.dt = dt;
+        nm.beta = b;
+        nm.gamma = g;
+        nm.ray_alpha = p->rayleigh_alpha;
+        nm.ray_beta = p->rayleigh_beta;
+        nm.ready = true;
+    });
+}
+
+int pfg_newmark_set_state(pfg_solver *h, int64_t n, const double *u, const double *v, const double *a)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->nm.ready, PFG_E_STATE, "Newmark: set-up first");
+        need(n == h->K.ndof(), PFG_E_ARG, "Newmark: state size differs from the system");
+        if (u) PFG_CUDA(cudaMemcpyAsync(h->nm.u.p, u, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        if (v) PFG_CUDA(cudaMemcpyAsync(h->nm.v.p, v, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        if (a) PFG_CUDA(cudaMemcpyAsync(h->nm.a.p, a, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_newmark_step(pfg_solver *h, const pfg_solve_opts *opts, int64_t n, const double *a_ext, double *u_out,
+                     double *v_out, double *a_out, pfg_info *info)
+{
+    SolveResult res;
+    const int rc = guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        auto &nm = h->nm;
+        need(nm.ready, PFG_E_STATE, "Newmark: set-up first");
+        need(n == h->K.ndof(), PFG_E_ARG, "Newmark: vector size differs from the system");
+        DevMatrix *Kp = find_slot(h, "A"), *Mp = find_slot(h, "B");
+        need(Kp && Mp, PFG_E_STATE, "Newmark: the kept stiffness / mass are gone");
+        const double b = nm.beta, g = nm.gamma, dt = nm.dt;
+        // getNewmarkBetaVector (SeismicAnalysisClass.f90:1478-1499):
+        //   R = M a_ext + M (u/(b dt^2) + v/(b dt) + (1/(2b) - 1) a)
+        //     + C (g/(b dt) u + (g/b - 1) v + dt (g/(2b) - 1) a),   C = alpha M + beta K
+        const double du = g / (b * dt), dv = g / b - 1.0, da = dt * (g / (2.0 * b) - 1.0);
+        const double mu = 1.0 / (b * dt * dt) + nm.ray_alpha * du, mv = 1.0 / (b * dt) + nm.ray_alpha * dv,
+                     ma = 1.0 / (2.0 * b) - 1.0 + nm.ray_alpha * da;
+        const double ku = nm.ray_beta * du, kv = nm.ray_beta * dv, ka = nm.ray_beta * da;
+        const int gv = grid_for(n, 256, 152 * 16);
+        if (a_ext) PFG_CUDA(cudaMemcpyAsync(nm.tmp.p, a_ext, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        k_newmark_weights<<<gv, 256, 0, h->st>>>(n, a_ext ? nm.tmp.p : nullptr, nm.u.p, nm.v.p, nm.a.p, mu, mv, ma,
+                                                 ku, kv, ka, nm.wM.p, nm.wK.p);
+        PFG_CUDA(cudaGetLastError());
+        Krylov::spmv64(*Mp, nm.wM.p, nm.rhs.p, h->st);
+        Krylov::spmv64(*Kp, nm.wK.p, nm.tmp.p, h->st);
+        k_newmark_rhs<<<gv, 256, 0, h->st>>>(n, nm.rhs.p, nm.tmp.p, nm.base.p, h->have_fix ? h->fixed_d.p : nullptr);
+        PFG_CUDA(cudaGetLastError());
+        // A_eff u' = rhs from the previous displacement
+        PFG_CUDA(cudaMemcpyAsync(nm.x.p, nm.u.p, n * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+        KConfig cfg = to_config(opts);
+        if (!opts) {
+            cfg.algorithm = PFG_ALG_CG;
+            cfg.precond = PFG_PC_BLOCK_JACOBI;
+            cfg.stop_rule = PFG_STOP_TRUE_RELATIVE;
+        }
+        res = h->kry.solve(h->K, nm.rhs.p, nm.x.p, cfg, h->st);
+        if (h->have_fix) restore_fixed(n, nm.x.p, h->fixed_d.p, h->fixval_d.p, h->st);
+        k_newmark_update<<<gv, 256, 0, h->st>>>(n, nm.x.p, nm.u.p, nm.v.p, nm.a.p, b, g, dt);
+        PFG_CUDA(cudaGetLastError());
+        if (u_out) PFG_CUDA(cudaMemcpyAsync(u_out, nm.u.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        if (v_out) PFG_CUDA(cudaMemcpyAsync(v_out, nm.v.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        if (a_out) PFG_CUDA(cudaMemcpyAsync(a_out, nm.a.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+        fill_info(info, res, cfg.precision);
+    });
+    if (rc != PFG_OK) return rc;
+    return solve_status(res);
+}
+
+}  // extern "C"

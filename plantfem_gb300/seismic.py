@@ -1,0 +1,93 @@
+"""SeismicAnalysis: linear Newmark-beta time stepping with Rayleigh damping.
+
+Mirrors the fields and the step of plantFEM's ``SeismicAnalysis_``
+(SeismicAnalysisClass.f90: defaults :98-109, ``LinearReyleighNewmark``
+:1255-1436, Newmark formulas :1464-1535) over the GPU path: the stiffness and
+consistent mass are assembled once on the device, combined into the Newmark
+matrix, and every call of :meth:`LinearReyleighNewmark` advances one time step
+(two SpMVs, one warm-started solve and the velocity/acceleration update on the
+GPU; ``pfg_newmark_*`` in include/pfg.h).  The reference re-integrates every
+element matrix at every step; the results are the same linear algebra.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .femdomain import FEMDomain
+from .femsolver import FEMSolver
+
+
+class SeismicAnalysis:
+    # SeismicAnalysis_ public parameters (SeismicAnalysisClass.f90:98-109)
+    dt: float = 1.0
+    alpha: float = 0.524      # Rayleigh damping C = alpha M + beta K
+    beta: float = 0.00129
+    Newmark_beta: float = 0.25
+    Newmark_gamma: float = 0.5
+
+    def __init__(self):
+        self.femdomain: FEMDomain | None = None
+        self.Density = self.YoungModulus = self.PoissonRatio = None
+        self.fixes: list[tuple[np.ndarray, np.ndarray]] = []
+        self.U = self.V = self.A = self.A_ext = None
+        self._s: FEMSolver | None = None
+        self.last_info: dict = {}
+
+    def init(self, femdomain: FEMDomain, Density, YoungModulus, PoissonRatio) -> "SeismicAnalysis":
+        self.femdomain = femdomain
+        ne = femdomain.ne()
+        self.Density = np.broadcast_to(np.asarray(Density, dtype=np.float64), (ne,)).copy()
+        self.YoungModulus = np.broadcast_to(np.asarray(YoungModulus, dtype=np.float64), (ne,)).copy()
+        self.PoissonRatio = np.broadcast_to(np.asarray(PoissonRatio, dtype=np.float64), (ne,)).copy()
+        n = 3 * femdomain.nn()
+        self.U, self.V, self.A, self.A_ext = (np.zeros(n) for _ in range(4))
+        self._s = None
+        return self
+
+    def fixDisplacement(self, NodeList, direction: str, disp: float = 0.0):
+        """Prescribed displacement of nodes (1-based ids) in x, y or z
+        (FixNodeList_x/y/z with FixNodeList_Disp_*)."""
+        d = {"x": 0, "y": 1, "z": 2}[direction]
+        ids = 3 * (np.asarray(NodeList, dtype=np.int64) - 1) + d + 1
+        self.fixes.append((ids.astype(np.int32), np.full(ids.shape[0], float(disp))))
+        self._s = None
+
+    def _setup(self):
+        s = FEMSolver()
+        s.setDomain(self.femdomain)
+        s.setCRS(3)
+        s.assembleMass(self.Density)
+        s.keepThisMatrixAs("B")
+        s.zeros()
+        s.assembleStiffness(self.YoungModulus, self.PoissonRatio)
+        s.keepThisMatrixAs("A")
+        for ids, vals in self.fixes:
+            s.fix(1, ids, FixValues=vals)
+        p = N.NewmarkParams(float(self.dt), float(self.Newmark_beta), float(self.Newmark_gamma), float(self.alpha),
+                            float(self.beta))
+        N.check(s._lib.pfg_newmark_setup(s.handle, C.byref(p)))
+        n = self.U.shape[0]
+        N.check(s._lib.pfg_newmark_set_state(s.handle, n, self.U.ctypes.data, self.V.ctypes.data,
+                                             self.A.ctypes.data))
+        self._s = s
+        self._key = (self.dt, self.Newmark_beta, self.Newmark_gamma, self.alpha, self.beta)
+
+    def LinearReyleighNewmark(self, TOL: float = 1e-10, precision: str = "fp64", storage: str = "full"):
+        """One time step (SeismicAnalysis_%LinearReyleighNewmark): U, V, A advance
+        with the external acceleration A_ext; the solve stops at |R - A_eff U|/|R| <= TOL."""
+        key = (self.dt, self.Newmark_beta, self.Newmark_gamma, self.alpha, self.beta)
+        if self._s is None or self._key != key:
+            self._setup()
+        s = self._s
+        opts = s._opts("CG", precision, "BlockJacobi", "true_relative", storage=storage)
+        opts.relative_er = float(TOL)
+        n = self.U.shape[0]
+        ae = np.ascontiguousarray(self.A_ext, dtype=np.float64)
+        info = N.Info()
+        N.check(s._lib.pfg_newmark_step(s.handle, C.byref(opts), n, ae.ctypes.data, self.U.ctypes.data,
+                                        self.V.ctypes.data, self.A.ctypes.data, C.byref(info)))
+        self.last_info = info.as_dict()
+        return self.U
