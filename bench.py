@@ -15,7 +15,8 @@ reference's bicgstab_CRS_2 timed on the host cores, and the two other forms
 against the plain path on the same GPU: 512 uneven thin slabs solved in one
 persistent batched launch (``batched_slabs``) and the adjoint dL/dE of a 64^3
 mesh with 262,144 per-element moduli (``adjoint``); and the modal analysis of
-the 60^3 cantilever by LOBPCG, FP64 vs mixed (``modal_lobpcg``).
+the 60^3 cantilever by LOBPCG, FP64 vs mixed (``modal_lobpcg``), and its
+Newmark-beta time stepping (``newmark``).
 
 ``--impl reference`` times the reference algorithm itself on the host CPU
 (the oracle's restatement of bicgstab_CRS_2 with the per-nonzero OpenMP
@@ -322,6 +323,44 @@ def modal_lines(n=60, nev=20, block=24, tol=1e-8):
     return out
 
 
+def newmark_lines(n=60, steps=40, dt=1e-3):
+    """Linear Newmark-beta time stepping (SeismicAnalysis_%LinearReyleighNewmark):
+    the n^3 cantilever of the modal workload (x = 0 clamped, rho 1e3, E 1e4,
+    nu 0.3, Rayleigh alpha 0.524 / beta 0.00129, Newmark 0.25 / 0.5) under a
+    z acceleration of -9.8; `steps` steps of dt, each solved to 1e-10 from the
+    previous displacement; FP64 vs mixed (symmetric FP32 copy)."""
+    from plantfem_gb300 import SeismicAnalysis, problems
+    p = problems.cantilever(n)
+    dom = p["domain"]
+    out = {"workload": f"cantilever{n}: {3 * dom.nn()} DOF, {steps} steps of dt {dt:g}, CG + block Jacobi to 1e-10"}
+    res = {}
+    for prec, storage in (("fp64", "full"), ("mixed", "symmetric")):
+        sa = SeismicAnalysis().init(dom, p["rho"], p["E"], p["nu"])
+        sa.dt = dt
+        nodes = np.nonzero(dom.nodcoord[:, 0] <= 0.0)[0] + 1
+        for d in "xyz":
+            sa.fixDisplacement(nodes, d, 0.0)
+        a_ext = np.zeros(3 * dom.nn())
+        a_ext[2::3] = -9.8
+        sa.A_ext = a_ext
+        sa.LinearReyleighNewmark(TOL=1e-10, precision=prec, storage=storage)  # set-up and first step
+        t = time.perf_counter()
+        its = 0
+        for _ in range(steps):
+            sa.LinearReyleighNewmark(TOL=1e-10, precision=prec, storage=storage)
+            its += sa.last_info["iterations"]
+        wall = (time.perf_counter() - t) / steps
+        res[prec] = sa.U.copy()
+        out[prec] = {"ms_per_step": round(wall * 1e3, 3), "steps_per_s": round(1.0 / wall, 2),
+                     "mean_iterations": round(its / steps, 1), "status": sa.last_info["status"],
+                     "tip_uz": float(sa.U[2::3].min())}
+        _progress(f"newmark {prec}: {wall * 1e3:.1f} ms/step")
+    out["max_rel_diff_mixed_vs_fp64"] = float(np.linalg.norm(res["mixed"] - res["fp64"]) /
+                                              np.linalg.norm(res["fp64"]))
+    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"], 3)
+    return out
+
+
 def batch_lines(count=512, tol=1e-8, seed=5):
     """Batched uneven organs: `count` thin slabs nx x ny x nz (nx, ny ~ U{8..64},
     nz ~ U{1..3}, numpy seed 5), E lognormal per slab, nu 0.3, one short edge
@@ -521,6 +560,11 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
         except Exception as e:
             out_extra["modal_lobpcg"] = {"error": str(e)}
         _progress("modal analysis done")
+    if not args.skip_newmark and rank == 0:
+        try:
+            out_extra["newmark"] = newmark_lines()
+        except Exception as e:
+            out_extra["newmark"] = {"error": str(e)}
     if not args.skip_batch and rank == 0:
         try:
             out_extra["batched_slabs"] = batch_lines(args.batch_count)
@@ -664,6 +708,7 @@ def main():
     ap.add_argument("--skip-batch", action="store_true", help="skip the 512-slab batched solve lines")
     ap.add_argument("--batch-count", type=int, default=512, help="slabs in the batched solve lines")
     ap.add_argument("--skip-adjoint", action="store_true", help="skip the 64^3 adjoint lines")
+    ap.add_argument("--skip-newmark", action="store_true", help="skip the Newmark-beta time-stepping lines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
