@@ -197,6 +197,9 @@ int pfg_keep_this_matrix_as(pfg_solver *h, const char *name);
 
 /* FEMSolver_%fix_eig(IDs) (FEMSolverClass.f90:1607-1628): 1-based DOF ids whose
  * amplitude is zero in eig; accumulated, duplicates ignored. */
+/* FEMSolver_%loadMatrix(from) (FEMSolverClass.f90:1203-1222): the matrix kept
+ * under `name` becomes the working matrix again (pattern and values). */
+int pfg_load_matrix(pfg_solver *h, const char *name);
 int pfg_fix_eig(pfg_solver *h, int64_t n, const int32_t *ids);
 
 #define PFG_EIG_STOP_REFERENCE 0 /* max|R| / max|R at iteration 1| < tol, SparseClass.f90:2218-2234 */

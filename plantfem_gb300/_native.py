@@ -119,6 +119,7 @@ SIGNATURES = {
     "pfg_profile_kernel": (C.c_int, [_P, _i32, _i32, C.POINTER(_d), C.POINTER(_d)]),
     "pfg_keep_this_matrix_as": (C.c_int, [_P, C.c_char_p]),
     "pfg_fix_eig": (C.c_int, [_P, _i64, _P]),
+    "pfg_load_matrix": (C.c_int, [_P, C.c_char_p]),
     "pfg_eig_opts_default": (None, [C.POINTER(EigOpts)]),
     "pfg_eig": (C.c_int, [_P, C.POINTER(EigOpts), _i32, _P, _P, C.POINTER(Info)]),
     "pfg_linear_solver_crs_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _i64, C.POINTER(SolveOpts), C.POINTER(Info),

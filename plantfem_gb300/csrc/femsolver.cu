@@ -711,6 +711,20 @@ int pfg_keep_this_matrix_as(pfg_solver *h, const char *name)
     });
 }
 
+int pfg_load_matrix(pfg_solver *h, const char *name)
+{
+    return guard([&] {
+        need(h && name, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        flush_pending(h);
+        DevMatrix *slot = find_slot(h, name);
+        need(slot != nullptr, PFG_E_ARG, "loadMatrix: no matrix kept under that name");
+        copy_matrix(*slot, h->K, h->st);
+        h->have_crs = true;
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
 int pfg_fix_eig(pfg_solver *h, int64_t n, const int32_t *ids)
 {
     return guard([&] {

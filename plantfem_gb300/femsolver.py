@@ -252,6 +252,22 @@ class FEMSolver:
         """FEMSolver_%keepThisMatrixAs (FEMSolverClass.f90:1544-1604)."""
         N.check(self._lib.pfg_keep_this_matrix_as(self._h, As.encode()))
 
+    def loadMatrix(self, from_: str):
+        """FEMSolver_%loadMatrix(from) (FEMSolverClass.f90:1203-1222): the matrix
+        kept as "A" or "B" becomes the working matrix."""
+        N.check(self._lib.pfg_load_matrix(self._h, from_.encode()))
+
+    def saveMatrix(self, name: str, CRS_as_dense: bool = False, zero_or_nonzero: bool = False):
+        """FEMSolver_%saveMatrix (FEMSolverClass.f90:1225-1306): the working matrix
+        as name_data.txt / name_indices.txt / name_indptr.txt (one entry per
+        line, 1-based indices), or as name_dense.csv."""
+        from .crs_io import write_crs_files, write_dense_csv
+        rp, ci, v = self.getCRS()
+        if CRS_as_dense:
+            write_dense_csv(name + "_dense.csv", rp, ci, v, zero_or_nonzero)
+        else:
+            write_crs_files(name, rp, ci, v)
+
     def fix_eig(self, IDs):
         """FEMSolver_%fix_eig (FEMSolverClass.f90:1607-1628)."""
         ids = _i32(IDs)
