@@ -57,6 +57,58 @@ class FEMDomain:
             self.nodcoord[:, d] = (L / span) * self.nodcoord[:, d]
         return self
 
+    def vtk(self, name: str, scalar=None, vector=None, tensor=None, field: str | None = None, displacement=None):
+        """FEMDomain_%vtk (FEMDomainClass.f90:8362 onwards): legacy ASCII VTK of the
+        hex8 mesh (cell type 12, 0-based connectivity) with an optional point or
+        cell scalar / vector / tensor field (its length picks points or cells);
+        ``displacement`` writes the deformed mesh (the domain itself is not changed)."""
+        if displacement is not None:
+            d = np.asarray(displacement, dtype=np.float64).reshape(self.nn(), 3)
+            saved = self.nodcoord
+            self.nodcoord = saved + d
+            try:
+                return self.vtk(name, scalar, vector, tensor, field)
+            finally:
+                self.nodcoord = saved
+        path = name if name.lower().endswith(".vtk") else name + ".vtk"
+        nn, ne, nne = self.nn(), self.ne(), self.elemnod.shape[1]
+        lines = ["# vtk DataFile Version 2.0", name, "ASCII", "DATASET UNSTRUCTURED_GRID", f"POINTS {nn} float"]
+        lines += [" ".join(repr(float(c)) for c in row) for row in self.nodcoord]
+        lines.append(f"CELLS {ne} {ne * (nne + 1)}")
+        lines += [f"{nne} " + " ".join(str(int(k) - 1) for k in row) for row in self.elemnod]
+        lines.append(f"CELL_TYPES {ne}")
+        lines += ["12"] * ne
+
+        def block(arr, kind):
+            arr = np.asarray(arr, dtype=np.float64)
+            n0 = arr.shape[0]
+            if n0 == nn:
+                where, label = f"POINT_DATA {nn}", f"point_{kind}"
+            elif n0 == ne:
+                where, label = f"CELL_DATA {ne}", f"cell_{kind}"
+            else:
+                raise ValueError(f"{kind}: {n0} rows, expected nn = {nn} or ne = {ne}")
+            label = field or label
+            out = [where]
+            if kind == "scalars":
+                out += [f"SCALARS {label} float", "LOOKUP_TABLE default"]
+                out += [repr(float(v)) for v in arr]
+            elif kind == "vectors":
+                out.append(f"VECTORS {label} float")
+                out += [" ".join(repr(float(v)) for v in row) for row in arr.reshape(n0, -1)]
+            else:
+                out.append(f"TENSORS {label} float")
+                for t in arr.reshape(n0, 3, 3):
+                    out += [" ".join(repr(float(v)) for v in r) for r in t]
+            return out
+
+        for arr, kind in ((scalar, "scalars"), (vector, "vectors"), (tensor, "tensors")):
+            if arr is not None:
+                lines += block(arr, kind)
+        with open(path, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        return path
+
     def deform(self, disp) -> "FEMDomain":
         """nodcoord += reshape(disp, nn, nd) with plantFEM's row-major reshape
         (FEMDomainClass.f90:14482, ArrayClass.f90:5328-5344)."""

@@ -16,3 +16,21 @@ def test_crs_files_round_trip(tmp_path):
     assert open(name + "_indices.txt").readline() == "1 \n"
     write_dense_csv(str(tmp_path / "K_dense.csv"), rp, ci, v, zero_or_nonzero=True)
     assert open(str(tmp_path / "K_dense.csv")).read().splitlines() == ["*,0,*", "0,*,0", "*,0,*"]
+
+
+def test_vtk_hex8_mesh_with_fields(tmp_path):
+    from plantfem_gb300 import FEMDomain
+    dom = FEMDomain().create("Cube3D", 2, 1, 1)
+    disp = np.zeros(3 * dom.nn())
+    disp[2::3] = 0.5
+    path = dom.vtk(str(tmp_path / "m"), scalar=np.arange(dom.ne(), dtype=float),
+                   vector=np.ones((dom.nn(), 3)), displacement=disp)
+    txt = open(path).read().splitlines()
+    assert txt[0] == "# vtk DataFile Version 2.0" and txt[4] == f"POINTS {dom.nn()} float"
+    pts = np.array([[float(v) for v in ln.split()] for ln in txt[5:5 + dom.nn()]])
+    assert np.allclose(pts, dom.nodcoord + disp.reshape(-1, 3))  # deformed on output only
+    k = 5 + dom.nn()
+    assert txt[k] == f"CELLS {dom.ne()} {dom.ne() * 9}"
+    assert txt[k + 1].split() == ["8"] + [str(int(c) - 1) for c in dom.elemnod[0]]
+    assert f"CELL_DATA {dom.ne()}" in txt and f"POINT_DATA {dom.nn()}" in txt and "CELL_TYPES 2" in txt
+    assert np.allclose(dom.nodcoord.max(axis=0), [1.0, 1.0, 1.0])  # domain unchanged
