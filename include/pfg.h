@@ -59,6 +59,16 @@ extern "C" {
 #define PFG_PC_NONE 0           /* unpreconditioned, as the reference */
 #define PFG_PC_JACOBI 1         /* point Jacobi (JacobiPreconditionerCRS, FEMSolverClass.f90:2508-2529) */
 #define PFG_PC_BLOCK_JACOBI 2   /* inverse of each 3x3 diagonal node block */
+/* ILU(0) (FEMSolver_%solve(preconditioning="ILU"|"incompleteLU"),
+ * FEMSolverClass.f90:1777-1784 -> bicgstab_CRS_ILU, LinearSolverClass.f90:4104-4230):
+ * BiCGSTAB only, FP64 only, right-preconditioned by D^-1 L^-1 of the ILU(0)
+ * factor (ILU_matvecCRS, SparseClass.f90:1795-1852, as it executes).  The
+ * factor is taken once per pattern and kept across solves (ILU_MATRIX);
+ * pfg_ilu_reset drops it. */
+#define PFG_PC_ILU0 3           /* ILUCRS exactly: each row's k in stored column order */
+#define PFG_PC_ILU0_SORTED 4    /* ILUCRS with each row's k in ascending column order (the order
+                                   SparseClass.f90:1671 asks for; equal to PFG_PC_ILU0 for rows
+                                   whose columns are sorted) */
 
 #define PFG_STOP_REFERENCE 0    /* sqrt(rr/rr_1) < relative_er or sqrt(rr) < er0, FEMSolverClass.f90:2275-2289 */
 #define PFG_STOP_TRUE_RELATIVE 1 /* |b - A x| / |b| <= relative_er, with |b - A x| recomputed in FP64 */
@@ -188,6 +198,24 @@ int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop
  * x(fixed) = value.  opts NULL -> pfg_solve_opts_default.  x0 may be NULL.
  * x_out receives n values; info may be NULL. */
 int pfg_solve(pfg_solver *h, const pfg_solve_opts *opts, const double *x0, double *x_out, pfg_info *info);
+
+/* Drop the ILU(0) factor the handle keeps for PFG_PC_ILU0* solves (the
+ * reference keeps FEMSolver_%ILU_MATRIX for good, FEMSolverClass.f90:67,
+ * LinearSolverClass.f90:4126-4135): the next ILU solve factors again. */
+int pfg_ilu_reset(pfg_solver *h);
+
+/* ILUCRS(0) (SparseClass.f90:1629-1792) of the working matrix as it is now
+ * (call pfg_eliminate first for the matrix pfg_solve factors), unless the
+ * handle holds the factor of this pattern for the same order already.
+ * sorted: 0 stored column order (PFG_PC_ILU0), 1 ascending (PFG_PC_ILU0_SORTED).
+ * lu_out (may be NULL): nnz values on the pattern pfg_get_crs returns, unit
+ * lower factor strictly below the diagonal, U on and above it. */
+int pfg_ilu_factor(pfg_solver *h, int32_t sorted, double *lu_out);
+
+/* out = D^-1 L^-1 v with the held factor (ILU_matvecCRS, SparseClass.f90:1795-1852,
+ * as it executes); factors in ascending order first if none is held.  Host
+ * vectors of pfg ndof values. */
+int pfg_ilu_apply(pfg_solver *h, const double *v, double *out);
 
 /* ------------------------------------------------------------- eigenproblem */
 /* FEMSolver_%keepThisMatrixAs(As) (FEMSolverClass.f90:1544-1604): copy the

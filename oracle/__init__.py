@@ -72,6 +72,10 @@ def lib():
     L.orc_reduce_crs.argtypes = [C.c_int64, _i64, _i32, _d, C.c_int64, _i32, C.c_void_p,
                                  C.c_void_p, C.c_void_p]
     L.orc_reduce_crs.restype = C.c_int64
+    L.orc_ilu0.argtypes = [C.c_int64, _i64, _i32, _d, C.c_int]
+    L.orc_ilu_apply.argtypes = [C.c_int64, _i64, _i32, _d, _d, _d]
+    L.orc_bicgstab_ilu.argtypes = [C.c_int64, _i64, _i32, _d, _d, _d, _d, C.c_int, C.c_double, C.c_double,
+                                   C.POINTER(C.c_int)]
     L.orc_num_threads.restype = C.c_int
     _LIB = L
     return L
@@ -236,6 +240,36 @@ def bicgstab_crs2(row_ptr, col_idx, val, b, x0=None, itrmax=100000, er0=1e-10, r
     it = C.c_int(0)
     rc = lib().orc_bicgstab_crs2(n, row_ptr, col_idx, val, x, np.ascontiguousarray(b, dtype=np.float64),
                                  itrmax, er0, relative_er, int(atomic), C.byref(it))
+    return x, rc, it.value
+
+
+def ilu0(row_ptr, col_idx, val, sorted=False):
+    """ILUCRS(0) (SparseClass.f90:1629-1792) of a 1-based CRS -> factor values
+    on the same pattern (unit lower L strictly below, U on and above the
+    diagonal).  sorted=False visits each row's k in stored column order, as
+    the reference does; sorted=True in ascending column order."""
+    lu = np.array(val, dtype=np.float64)
+    lib().orc_ilu0(row_ptr.shape[0] - 1, row_ptr, col_idx, lu, int(bool(sorted)))
+    return lu
+
+
+def ilu_apply(row_ptr, col_idx, lu, v):
+    """ILU_matvecCRS (SparseClass.f90:1795-1852) as executed: D^-1 L^-1 v."""
+    out = np.zeros(row_ptr.shape[0] - 1)
+    lib().orc_ilu_apply(out.shape[0], row_ptr, col_idx, lu, np.ascontiguousarray(v, dtype=np.float64), out)
+    return out
+
+
+def bicgstab_ilu(row_ptr, col_idx, val, b, lu=None, sorted=False, x0=None, itrmax=100000, er0=1e-10,
+                 relative_er=1e-10):
+    """bicgstab_CRS_ILU (LinearSolverClass.f90:4104-4230) -> (x, rc, iterations)."""
+    n = b.shape[0]
+    if lu is None:
+        lu = ilu0(row_ptr, col_idx, val, sorted)
+    x = np.zeros(n) if x0 is None else np.array(x0, dtype=np.float64)
+    it = C.c_int(0)
+    rc = lib().orc_bicgstab_ilu(n, row_ptr, col_idx, val, lu, x, np.ascontiguousarray(b, dtype=np.float64),
+                                itrmax, er0, relative_er, C.byref(it))
     return x, rc, it.value
 
 

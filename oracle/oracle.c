@@ -748,3 +748,146 @@ int orc_num_threads(void)
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* A18 ILUCRS(fill_in_order = 0) (SparseClass.f90:1629-1792, case (0)): the  */
+/* in-place incomplete LU factorization on the CRS pattern.  diag_vec starts */
+/* as the matrix diagonal (diagCRS :1597-1626, 0 where a row stores none);    */
+/* for rows i = 2..n, every entry k < i of row i in turn:                     */
+/*     A_ik = get(i,k) / diag_vec(k);  update(i,k) = A_ik;                    */
+/*     add(i,j, -A_ik * get(k,j)) for the entries j >= k+1 of row i;          */
+/*     diag_vec(i) = get(i,i).                                                 */
+/* get of an entry row k does not store is 0 (getCRS :1542-1560).  The k of a */
+/* row are visited in the row's STORED column order (:1664-1672; the comment */
+/* there asks for sorted columns): sorted = 0 restates that, sorted != 0     */
+/* visits them in ascending column order, which is the same thing for rows  */
+/* whose columns are sorted and the textbook ILU(0) for any row.             */
+/* ------------------------------------------------------------------------ */
+void orc_ilu0(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, double *val, int sorted)
+{
+    double *diag = calloc((size_t)n, sizeof(double));
+    int64_t *posk = malloc((size_t)n * sizeof(int64_t));
+    int64_t maxlen = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        posk[i] = -1;
+        const int64_t s = row_ptr[i] - 1, e = row_ptr[i + 1] - 1;
+        if (e - s > maxlen) maxlen = e - s;
+        for (int64_t q = s; q < e; ++q)
+            if (col_idx[q] - 1 == i) { diag[i] = val[q]; break; }
+    }
+    int64_t *seq = malloc((size_t)(maxlen > 0 ? maxlen : 1) * sizeof(int64_t));
+    for (int64_t i = 1; i < n; ++i) {
+        const int64_t s = row_ptr[i] - 1, e = row_ptr[i + 1] - 1, len = e - s;
+        for (int64_t q = 0; q < len; ++q) seq[q] = s + q;
+        if (sorted) /* insertion sort of the entry positions by column (stable) */
+            for (int64_t q = 1; q < len; ++q) {
+                const int64_t t = seq[q];
+                int64_t r = q;
+                while (r > 0 && col_idx[seq[r - 1]] > col_idx[t]) { seq[r] = seq[r - 1]; --r; }
+                seq[r] = t;
+            }
+        for (int64_t qq = 0; qq < len; ++qq) {
+            const int64_t kk = seq[qq];
+            const int64_t k = col_idx[kk] - 1;
+            if (k >= i) continue;
+            const double a_ik = val[kk] / diag[k];
+            val[kk] = a_ik;
+            const int64_t ks = row_ptr[k] - 1, ke = row_ptr[k + 1] - 1;
+            for (int64_t q = ke - 1; q >= ks; --q) posk[col_idx[q] - 1] = q; /* first match wins */
+            for (int64_t jj = s; jj < e; ++jj) {
+                const int64_t j = col_idx[jj] - 1;
+                if (j < k + 1) continue;
+                const double a_kj = posk[j] >= 0 ? val[posk[j]] : 0.0;
+                val[jj] = val[jj] + (-(a_ik * a_kj));
+            }
+            for (int64_t q = ks; q < ke; ++q) posk[col_idx[q] - 1] = -1;
+            double d = 0.0;
+            for (int64_t q = s; q < e; ++q)
+                if (col_idx[q] - 1 == i) { d = val[q]; break; }
+            diag[i] = d;
+        }
+    }
+    free(seq);
+    free(posk);
+    free(diag);
+}
+
+/* ILU_matvecCRS (SparseClass.f90:1795-1852) as it executes on an ILU(0)      */
+/* factor: forward substitution with the unit lower factor (:1803-1817),      */
+/* then division by the factor's diagonal, 0 taken as 1 (:1820-1828).  The    */
+/* loop written as the backward substitution (:1830-1849) ends each row by   */
+/* storing back the value it saved before the row's loop, so it leaves the   */
+/* vector as it was: the operator applied is D^-1 L^-1.                       */
+void orc_ilu_apply(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, const double *lu,
+                   const double *v, double *out)
+{
+    for (int64_t i = 0; i < n; ++i) out[i] = v[i];
+    for (int64_t i = 1; i < n; ++i) {
+        double s = out[i];
+        for (int64_t q = row_ptr[i] - 1; q < row_ptr[i + 1] - 1; ++q)
+            if (col_idx[q] - 1 < i) s = s - lu[q] * out[col_idx[q] - 1];
+        out[i] = s;
+    }
+    for (int64_t i = 0; i < n; ++i) {
+        double d = 0.0;
+        for (int64_t q = row_ptr[i] - 1; q < row_ptr[i + 1] - 1; ++q)
+            if (col_idx[q] - 1 == i) { d = lu[q]; break; }
+        if (d == 0.0) d = 1.0;
+        out[i] = out[i] / d;
+    }
+}
+
+/* bicgstab_CRS_ILU (LinearSolverClass.f90:4104-4230): BiCGSTAB right-       */
+/* preconditioned by the ILU(0) factor lu (orc_ilu0): y = A M^-1 p and        */
+/* v = A M^-1 e through sub_crs_matvec's precondition argument (:3751-3763), */
+/* x += alp M^-1 p + c3 M^-1 e.  Returns at once when |r0|^2 < er0 (:4150);  */
+/* stop rules, return codes and *iters as orc_bicgstab_crs2.                  */
+int orc_bicgstab_ilu(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, const double *a,
+                     const double *lu, double *x, const double *b, int itrmax, double er0, double relative_er,
+                     int *iters)
+{
+    double *r = malloc(n * sizeof(double)), *r0 = malloc(n * sizeof(double));
+    double *p = malloc(n * sizeof(double)), *y = malloc(n * sizeof(double));
+    double *e = malloc(n * sizeof(double)), *v = malloc(n * sizeof(double));
+    double *pd = malloc(n * sizeof(double)), *ps = malloc(n * sizeof(double));
+    int rc = 1, itr = 0;
+    double c1, c2, c3, alp, bet, ev, vv, rr, re_er0 = 1.0;
+    orc_sub_crs_matvec(n, row_ptr, col_idx, a, x, y, 0);
+    for (int64_t i = 0; i < n; ++i) r[i] = b[i] - y[i];
+    c1 = orc_dot(n, r, r);
+    if (c1 < er0) {
+        rc = 0;
+        goto done;
+    }
+    for (int64_t i = 0; i < n; ++i) { p[i] = r[i]; r0[i] = r[i]; }
+    for (itr = 1; itr <= itrmax; ++itr) {
+        c1 = orc_dot(n, r0, r);
+        orc_ilu_apply(n, row_ptr, col_idx, lu, p, pd);
+        orc_sub_crs_matvec(n, row_ptr, col_idx, a, pd, y, 0);
+        c2 = orc_dot(n, r0, y);
+        alp = c1 / c2;
+        for (int64_t i = 0; i < n; ++i) e[i] = r[i] - alp * y[i];
+        orc_ilu_apply(n, row_ptr, col_idx, lu, e, ps);
+        orc_sub_crs_matvec(n, row_ptr, col_idx, a, ps, v, 0);
+        ev = orc_dot(n, e, v);
+        vv = orc_dot(n, v, v);
+        if (vv == 0.0) { rc = -1; break; }
+        c3 = ev / vv;
+        for (int64_t i = 0; i < n; ++i) {
+            x[i] = x[i] + alp * pd[i] + c3 * ps[i];
+            r[i] = e[i] - c3 * v[i];
+        }
+        rr = orc_dot(n, r, r);
+        if (itr == 1) re_er0 = rr;
+        if (sqrt(rr / re_er0) < relative_er) { rc = 0; break; }
+        if (sqrt(rr) < er0) { rc = 0; break; }
+        c1 = orc_dot(n, r0, r);
+        bet = c1 / (c2 * c3);
+        if (c2 * c3 == 0.0) { rc = -1; break; }
+        for (int64_t i = 0; i < n; ++i) p[i] = r[i] + bet * (p[i] - c3 * y[i]);
+    }
+done:
+    if (iters) *iters = itr > itrmax ? itrmax : itr;
+    free(r); free(r0); free(p); free(y); free(e); free(v); free(pd); free(ps);
+    return rc;
+}

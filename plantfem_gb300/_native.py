@@ -24,6 +24,7 @@ ALG_BICGSTAB, ALG_CG = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 STORAGE_FULL, STORAGE_SYMMETRIC = 0, 1
 PC_NONE, PC_JACOBI, PC_BLOCK_JACOBI = 0, 1, 2
+PC_ILU0, PC_ILU0_SORTED = 3, 4  # ILU(0): stored / ascending column order
 STOP_REFERENCE, STOP_TRUE_RELATIVE = 0, 1
 
 
@@ -125,6 +126,9 @@ SIGNATURES = {
     "pfg_linear_solver_crs_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _i64, C.POINTER(SolveOpts), C.POINTER(Info),
                                                 _P]),
     "pfg_eliminate": (C.c_int, [_P]),
+    "pfg_ilu_reset": (C.c_int, [_P]),
+    "pfg_ilu_factor": (C.c_int, [_P, C.c_int32, _P]),
+    "pfg_ilu_apply": (C.c_int, [_P, _P, _P]),
     "pfg_element_stress": (C.c_int, [_P, _P, _i64, _P, _P, _i32, _P]),
     "pfg_dev_assemble_stiffness": (C.c_int, [_P, _i64, _P, _P, _P]),
     "pfg_dev_set_rhs": (C.c_int, [_P, _i64, _P, _P]),

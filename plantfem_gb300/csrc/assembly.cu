@@ -919,6 +919,16 @@ __global__ void k_export_b1(int64_t n, int64_t nnz, const int64_t *__restrict__ 
         if (col_idx) col_idx[k] = bcol[k] + 1;
 }
 
+void export_values(const DevMatrix &K, const double *bval, double *val, cudaStream_t st)
+{
+    if (K.bs == 3)
+        k_export_b3<<<grid_for(K.nb, 128, 152 * 16), 128, 0, st>>>(K.nb, K.rp.p, K.col.p, bval, nullptr, nullptr,
+                                                                   val);
+    else if (K.nnzb)
+        PFG_CUDA(cudaMemcpyAsync(val, bval, K.nnzb * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    PFG_CUDA(cudaGetLastError());
+}
+
 void export_crs(const DevMatrix &K, int64_t *row_ptr, int32_t *col_idx, double *val, cudaStream_t st)
 {
     if (K.bs == 3) {

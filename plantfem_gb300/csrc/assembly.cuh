@@ -65,6 +65,9 @@ void import_crs(int64_t n, int64_t nnz, const int64_t *row_ptr, const int32_t *c
                 DevMatrix &K, cudaStream_t st, bool allow_blocks = true);
 // Block layout -> scalar CRS (1-based, device arrays, reference column order).
 void export_crs(const DevMatrix &K, int64_t *row_ptr, int32_t *col_idx, double *val, cudaStream_t st);
+// Values in the matrix's block-row layout (bval, K's pattern) -> scalar CRS
+// values in the order export_crs writes (device pointers).
+void export_values(const DevMatrix &K, const double *bval, double *val, cudaStream_t st);
 
 // Exclusive prefix sum of n int64 values (out may alias in); returns the total.
 int64_t exclusive_scan(const int64_t *in, int64_t *out, int64_t n, cudaStream_t st);

@@ -15,6 +15,7 @@
 
 #include "assembly.cuh"
 #include "batch.cuh"
+#include "ilu.cuh"
 
 namespace pfg {
 
@@ -820,6 +821,49 @@ int pfg_eliminate(pfg_solver *h)
         need(h->have_crs, PFG_E_STATE, "eliminate before setCRS");
         flush_pending(h);
         apply_fix_device(h);
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_ilu_reset(pfg_solver *h)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        h->kry.ilu_reset();
+    });
+}
+
+int pfg_ilu_factor(pfg_solver *h, int32_t sorted, double *lu_out)
+{
+    return guard([&] {
+        need(h != nullptr, PFG_E_ARG, "NULL handle");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "ILU(0) before setCRS");
+        flush_pending(h);
+        const Ilu0 &f = h->kry.ilu_factor(h->K, sorted != 0, h->st);
+        if (lu_out) {
+            const int64_t nnz = h->K.nnzb * h->K.bs * h->K.bs;
+            DevBuf<double> v((size_t)std::max<int64_t>(nnz, 1));
+            export_values(h->K, f.lu(), v.p, h->st);
+            PFG_CUDA(cudaMemcpyAsync(lu_out, v.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        }
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
+int pfg_ilu_apply(pfg_solver *h, const double *v, double *out)
+{
+    return guard([&] {
+        need(h && v && out, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "ILU(0) before setCRS");
+        const int64_t n = h->ndof();
+        DevBuf<double> dv((size_t)n), dout((size_t)n);
+        PFG_CUDA(cudaMemcpyAsync(dv.p, v, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        const Ilu0 &f = h->kry.ilu_factor(h->K, true, h->st);
+        f.apply(dv.p, dout.p, nullptr, h->st);
+        PFG_CUDA(cudaMemcpyAsync(out, dout.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
         PFG_CUDA(cudaStreamSynchronize(h->st));
     });
 }

@@ -24,6 +24,7 @@
 #include <unordered_map>
 
 #include "krylov.cuh"
+#include "ilu.cuh"
 
 namespace pfg {
 
@@ -1110,6 +1111,18 @@ Krylov::~Krylov()
     if (host_state_) cudaFreeHost(host_state_);
 }
 
+const Ilu0 &Krylov::ilu_factor(const DevMatrix &A, bool sorted, cudaStream_t st)
+{
+    if (!ilu_) ilu_.reset(new Ilu0());
+    ilu_->factor(A, sorted, st);
+    return *ilu_;
+}
+
+void Krylov::ilu_reset()
+{
+    if (ilu_) ilu_->reset();
+}
+
 template <int BS, typename T>
 static void launch_spmv(const DevMatrix &A, BsrView<T> v, const T *x, T *y, cudaStream_t st)
 {
@@ -1226,7 +1239,7 @@ void block_jacobi(const DevMatrix &A, int precond, double *d64, float *d32, cuda
 
 void Krylov::build_precond(const DevMatrix &A, int precond, bool fp32, cudaStream_t st)
 {
-    if (precond == PFG_PC_NONE) return;
+    if (precond == PFG_PC_NONE || is_ilu(precond)) return;
     const size_t m = (size_t)std::max<int64_t>(A.nb * A.bs * A.bs, 1);
     dinv_.ensure(m);
     if (fp32) dinv32_.ensure(m);
@@ -1302,7 +1315,8 @@ uint64_t Krylov::graph_key(int kind, const DevMatrix &A, const void *x, const KC
                     u(dinv32_.p), u(ph_.p), u(eh_.p), u(ph32_.p), u(eh32_.p), u(partials_.p), u(partials32_.p), u(ticket_.p), u(state_.p),
                     (uint64_t)cfg.precond, (uint64_t)cfg.stop_rule, (uint64_t)cfg.graph_chunk, (uint64_t)cfg.itrmax,
                     (uint64_t)cfg.fuse, (uint64_t)cfg.storage, u(y4_.p), u(A.sptr_u.p), u(A.scol_u.p),
-                    u(A.s32_u.p), d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta)});
+                    u(A.s32_u.p), d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta),
+                    ilu_ ? ilu_->generation() : 0, u(ilu_ ? ilu_->lu() : nullptr)});
 }
 
 // One chunk of CG iterations.  fuse: p = z + beta p formed inside the SpMV
@@ -1376,6 +1390,39 @@ static int bicg_chunk(const SellView<T> &A, bool fuse, int chunk, int64_t nb, T 
     return (fuse ? 3 : 5) * chunk;
 }
 
+// One chunk of ILU(0)-preconditioned FP64 BiCGSTAB iterations
+// (bicgstab_CRS_ILU's loop body, LinearSolverClass.f90:4140-4228): the
+// direction and e passes without a preconditioner, ph = M^-1 p and
+// eh = M^-1 e by the level-scheduled sweep, the products y = A ph and
+// v = A eh, and the update x += alpha ph + c3 eh.
+template <int BS>
+static int bicg_chunk_ilu(const SellView<double> &A, const Ilu0 &ilu, int chunk, int64_t nb, double *x, double *r,
+                          double *r0, double *p, double *y, double *e, double *v, double *ph, double *eh, KState *S,
+                          double *pd, float *pf, unsigned *tk, int stop_rule, double er0, double tol, int itrmax,
+                          cudaStream_t st)
+{
+    const int64_t n = nb * BS;
+    const int g3 = resident_grid(k_bicg_update<BS, double>, (n + 31) / 32);
+    const int g1 = resident_grid(k_bicg_spmv1_u<BS, double>, A.ns);
+    const int g2 = resident_grid(k_bicg_spmv2_u<BS, double>, A.ns);
+    const int gd = resident_grid(k_bicg_dir<BS, double>, (nb + 31) / 32);
+    const int ge = resident_grid(k_bicg_e<BS, double>, (nb + 31) / 32);
+    int nk = 0;
+    for (int it = 0; it < chunk; ++it) {
+        k_bicg_dir<BS, double><<<gd, kThreads, 0, st>>>(nb, r, p, y, ph, nullptr, PFG_PC_NONE, S);
+        nk += ilu.apply(p, ph, S, st);
+        k_bicg_spmv1_u<BS, double><<<g1, kThreads, 0, st>>>(A, ph, r0, y, S, pd, pf, tk);
+        k_bicg_e<BS, double><<<ge, kThreads, 0, st>>>(nb, r, y, e, eh, nullptr, PFG_PC_NONE, S);
+        nk += ilu.apply(e, eh, S, st);
+        k_bicg_spmv2_u<BS, double><<<g2, kThreads, 0, st>>>(A, eh, e, v, S, pd, pf, tk);
+        k_bicg_update<BS, double><<<g3, kThreads, 0, st>>>(nb, x, r, r0, ph, ph, e, eh, v, S, pd, pf, tk, stop_rule,
+                                                          er0, tol, 0.1, itrmax);
+        nk += 5;
+    }
+    PFG_CUDA(cudaGetLastError());
+    return nk;
+}
+
 // One chunk of FP32 CG iterations with the symmetric (upper-half) matrix:
 // dir, product into q4 with <p, Ap> and alpha, update (reads and clears q4).
 static int cg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *x, float *r, float *z, float *p,
@@ -1431,7 +1478,9 @@ SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfi
     PFG_CHECK(A.nb > 0, PFG_E_STATE, "empty matrix");
     PFG_CHECK(cfg.algorithm == PFG_ALG_CG || cfg.algorithm == PFG_ALG_BICGSTAB, PFG_E_ARG, "unknown algorithm");
     PFG_CHECK(cfg.precision == PFG_PREC_FP64 || cfg.precision == PFG_PREC_MIXED, PFG_E_ARG, "unknown precision");
-    PFG_CHECK(cfg.precond >= PFG_PC_NONE && cfg.precond <= PFG_PC_BLOCK_JACOBI, PFG_E_ARG, "unknown precond");
+    PFG_CHECK(cfg.precond >= PFG_PC_NONE && cfg.precond <= PFG_PC_ILU0_SORTED, PFG_E_ARG, "unknown precond");
+    PFG_CHECK(!is_ilu(cfg.precond) || (cfg.algorithm == PFG_ALG_BICGSTAB && cfg.precision == PFG_PREC_FP64),
+              PFG_E_UNSUPPORTED, "ILU(0) preconditions FP64 BiCGSTAB only (bicgstab_CRS_ILU)");
     if (cfg.itrmax <= 0) cfg.itrmax = 100000;
     if (cfg.graph_chunk <= 0) cfg.graph_chunk = 32;
     if (cfg.precision == PFG_PREC_MIXED) cfg.stop_rule = PFG_STOP_TRUE_RELATIVE;
@@ -1563,6 +1612,11 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
 {
     SolveResult res;
     build_precond(A, cfg.precond, false, st);
+    const bool ilu = is_ilu(cfg.precond);
+    if (ilu) {
+        ilu_factor(A, cfg.precond == PFG_PC_ILU0_SORTED, st);
+        ++launches_;
+    }
     const int64_t n = A.ndof();
     const int g = row_grid(A.nb);
     const uint64_t key = graph_key(2, A, x, cfg);
@@ -1570,7 +1624,22 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
         if (graph_) cudaGraphExecDestroy(graph_);
         graph_ = nullptr;
         int nk = 0;
+        // an ILU iteration captures two sweeps of one launch per level: a
+        // few thousand graph nodes per chunk at most
+        const int ilu_chunk =
+            ilu ? std::max(1, std::min(cfg.graph_chunk, 4096 / (5 + 2 * ilu_->levels()))) : cfg.graph_chunk;
         auto body = [&]() {
+            if (ilu) {
+                nk = A.bs == 3 ? bicg_chunk_ilu<3>(A.sell<double>(), *ilu_, ilu_chunk, A.nb, x, r_.p, r0_.p, pA_.p,
+                                                   yA_.p, e_.p, v_.p, ph_.p, eh_.p, state_.p, partials_.p,
+                                                   partials32_.p, ticket_.p, cfg.stop_rule, cfg.er0,
+                                                   cfg.relative_er, cfg.itrmax, st)
+                               : bicg_chunk_ilu<1>(A.sell<double>(), *ilu_, ilu_chunk, A.nb, x, r_.p, r0_.p, pA_.p,
+                                                   yA_.p, e_.p, v_.p, ph_.p, eh_.p, state_.p, partials_.p,
+                                                   partials32_.p, ticket_.p, cfg.stop_rule, cfg.er0,
+                                                   cfg.relative_er, cfg.itrmax, st);
+                return;
+            }
             nk = A.bs == 3 ? bicg_chunk<3, double>(A.sell<double>(), cfg.fuse != 0, cfg.graph_chunk, A.nb, x, r_.p,
                                                    r0_.p, pA_.p, pB_.p, yA_.p, yB_.p, e_.p, v_.p, ph_.p, eh_.p,
                                                    dinv_.p, cfg.precond, state_.p,
@@ -1591,6 +1660,8 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
         double rel = true_residual(A, b, x, r_.p, st);
         res.rel_residual = rel;
         if (cfg.stop_rule == PFG_STOP_TRUE_RELATIVE && rel <= cfg.relative_er) break;
+        // bicgstab_CRS_ILU returns before its loop when |r|^2 < er0 (:4150)
+        if (ilu && cfg.stop_rule == PFG_STOP_REFERENCE && host_state_->true_rr < cfg.er0) break;
         PFG_CUDA(cudaMemsetAsync(pA_.p, 0, n * sizeof(double), st));
         PFG_CUDA(cudaMemsetAsync(pB_.p, 0, n * sizeof(double), st));
         PFG_CUDA(cudaMemsetAsync(yA_.p, 0, n * sizeof(double), st));
@@ -1859,7 +1930,30 @@ __global__ void k_fill(double *a, int64_t n, double v)
 
 void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
 {
-    PFG_CHECK(kernel >= 0 && kernel <= 8 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel >= 0 && kernel <= 9 && reps > 0, PFG_E_ARG, "bad profile request");
+    if (kernel == 9) {
+        // one D^-1 L^-1 sweep of the held ILU(0) factor (factored in
+        // ascending column order if none is held)
+        if (!ilu_ || !ilu_->ready()) ilu_factor(A, true, st);
+        const int64_t nd = A.ndof();
+        DevBuf<double> v(nd), o(nd);
+        k_fill<<<grid_for(nd, 256, sm_count() * 8), 256, 0, st>>>(v.p, nd, 1.0);
+        for (int w = 0; w < 3; ++w) ilu_->apply(v.p, o.p, nullptr, st);
+        cudaEvent_t e0, e1;
+        PFG_CUDA(cudaEventCreate(&e0));
+        PFG_CUDA(cudaEventCreate(&e1));
+        PFG_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r) ilu_->apply(v.p, o.p, nullptr, st);
+        PFG_CUDA(cudaEventRecord(e1, st));
+        PFG_CUDA(cudaEventSynchronize(e1));
+        float t = 0.f;
+        cudaEventElapsedTime(&t, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        ms = (double)t / reps;
+        bytes = ilu_->sweep_bytes();
+        return;
+    }
     PFG_CHECK(kernel < 7 || A.bs == 3, PFG_E_UNSUPPORTED, "the symmetric product is built for 3x3 blocks");
     const int64_t n = A.ndof();
     const double bs2 = (double)(A.bs * A.bs);

@@ -4,6 +4,9 @@
 // krylov.cu; the FEMSolver handle (femsolver.cu) owns one of each.
 #pragma once
 
+#include <atomic>
+#include <memory>
+
 #include "bsr.cuh"
 #include "sell.cuh"
 
@@ -78,6 +81,9 @@ struct DevMatrix {
     DevBuf<float> s32_u;
     bool sell_u_pattern = false, s32_u_valid = false;
 
+    // bumped whenever rp/col change: keys factors derived from the pattern
+    uint64_t pattern_gen = 0;
+
     int64_t ndof() const { return nb * bs; }
     // v64 changed: every derived copy is stale
     void values_changed() { v32_valid = s64_valid = s32_valid = s32_u_valid = false; }
@@ -86,6 +92,13 @@ struct DevMatrix {
     {
         values_changed();
         sell_pattern = sell_u_pattern = false;
+        pattern_gen = next_pattern_gen();
+    }
+    // process-wide counter: no two patterns (of any matrix) share a value
+    static uint64_t next_pattern_gen()
+    {
+        static std::atomic<uint64_t> counter{0};
+        return ++counter;
     }
     template <typename T>
     BsrView<T> view() const;
@@ -119,6 +132,10 @@ inline SellView<float> sell_upper(const DevMatrix &A)
 // row.  Implemented in krylov.cu.
 void block_jacobi(const DevMatrix &A, int precond, double *d64, float *d32, cudaStream_t st);
 
+class Ilu0;
+
+inline bool is_ilu(int precond) { return precond == PFG_PC_ILU0 || precond == PFG_PC_ILU0_SORTED; }
+
 class Krylov {
   public:
     Krylov();
@@ -136,6 +153,10 @@ class Krylov {
     // 1 FP32 sliced SpMV, 2 FP32 CG SpMV with fused direction update (sliced),
     // 3 FP64 block-row SpMV, 4 FP32 block-row SpMV.
     void profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes);
+    // The ILU(0) factor kept for PFG_PC_ILU0* solves (ilu.cuh); factored from
+    // A (if not held for A's pattern and this column order) by ilu_factor.
+    const Ilu0 &ilu_factor(const DevMatrix &A, bool sorted, cudaStream_t st);
+    void ilu_reset();
 
   private:
     void prepare(const DevMatrix &A, const KConfig &cfg, cudaStream_t st);
@@ -166,6 +187,7 @@ class Krylov {
     cudaGraphExec_t graph_ = nullptr;
     uint64_t graph_key_ = 0;
     int graph_kernels_ = 0;  // kernels captured in graph_
+    std::unique_ptr<Ilu0> ilu_;
     int launches_ = 0;       // launch count of the current solve
 };
 

@@ -125,6 +125,11 @@ class FEMSolver:
         N.check(self._lib.pfg_get_crs_size(self._h, C.byref(n), None))
         return n.value
 
+    def _nnz(self) -> int:
+        n, nnz = C.c_int64(), C.c_int64()
+        N.check(self._lib.pfg_get_crs_size(self._h, C.byref(n), C.byref(nnz)))
+        return nnz.value
+
     def setRHS(self, RHS):
         """FEMSolver_%setRHS (FEMSolverClass.f90:431-437)."""
         r = _f64(RHS)
@@ -180,11 +185,14 @@ class FEMSolver:
 
     # ------------------------------------------------------------- solving
     def _opts(self, algorithm, precision, preconditioning, stop_rule, update_mode=0, reliable_delta=None,
-              storage="full"):
+              storage="full", ilu_order="stored"):
         alg = {"BiCGSTAB": N.ALG_BICGSTAB, "CG": N.ALG_CG}[algorithm or "BiCGSTAB"]
         prec = {"fp64": N.PREC_FP64, "FP64": N.PREC_FP64, "mixed": N.PREC_MIXED}[precision]
+        ilu = {"stored": N.PC_ILU0, "sorted": N.PC_ILU0_SORTED}[ilu_order]
         pc = {None: N.PC_NONE, "None": N.PC_NONE, "PointJacobi": N.PC_JACOBI, "Jacobi": N.PC_JACOBI,
-              "BlockJacobi": N.PC_BLOCK_JACOBI}[preconditioning]
+              "BlockJacobi": N.PC_BLOCK_JACOBI, "ILU": ilu, "incompleteLU": ilu}[preconditioning]
+        if pc in (N.PC_ILU0, N.PC_ILU0_SORTED):
+            alg = N.ALG_BICGSTAB  # FEMSolverClass.f90:1777-1784: ILU always runs bicgstab_CRS_ILU
         if stop_rule is None:
             stop_rule = "reference" if prec == N.PREC_FP64 else "true_relative"
         sr = {"reference": N.STOP_REFERENCE, "true_relative": N.STOP_TRUE_RELATIVE}[stop_rule]
@@ -198,15 +206,20 @@ class FEMSolver:
 
     def solve(self, algorithm: str | None = None, preconditioning: str | None = None, x0=None,
               precision: str = "fp64", stop_rule: str | None = None, update_mode=0,
-              storage: str = "full") -> np.ndarray:
+              storage: str = "full", ilu_order: str = "stored") -> np.ndarray:
         """x = FEMSolver_%solve([algorithm], [preconditioning], [x0]) (FEMSolverClass.f90:1697-1825).
 
         Defaults reproduce the reference: unpreconditioned BiCGSTAB in FP64 with
         its stop rule.  ``algorithm="CG"``, ``preconditioning="BlockJacobi"`` and
-        ``precision="mixed"`` select the GB300 forms.  Breakdown raises
-        (the reference stops); itrmax is reported in ``last_info``.
+        ``precision="mixed"`` select the GB300 forms.  ``preconditioning="ILU"``
+        (or ``"incompleteLU"``) runs bicgstab_CRS_ILU: FP64 BiCGSTAB with the
+        ILU(0) factor kept on the solver; ``ilu_order="sorted"`` factors with
+        each row's columns in ascending order (``"stored"``: the row's own
+        order, as ILUCRS).  Breakdown raises (the reference stops); itrmax is
+        reported in ``last_info``.
         """
-        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, storage=storage)
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, storage=storage,
+                          ilu_order=ilu_order)
         n = self.ndof()
         x = np.zeros(n)
         xi = None if x0 is None else _f64(x0)
@@ -214,6 +227,25 @@ class FEMSolver:
         N.check(self._lib.pfg_solve(self._h, C.byref(opts), N.ptr(xi), N.ptr(x), C.byref(info)))
         self.last_info = info.as_dict()
         return x
+
+    def ILU(self, sorted: bool = False) -> np.ndarray:
+        """ILUCRS(0) (SparseClass.f90:1629-1792) of the stored matrix, kept on the
+        solver for ILU solves -> the factor's values on getCRS()'s pattern."""
+        lu = np.zeros(self._nnz())
+        N.check(self._lib.pfg_ilu_factor(self._h, int(bool(sorted)), N.ptr(lu)))
+        return lu
+
+    def ILU_matvec(self, old_vector) -> np.ndarray:
+        """ILU_matvecCRS (SparseClass.f90:1795-1852) with the kept factor, as it
+        executes: D^-1 L^-1 old_vector."""
+        v = _f64(old_vector)
+        out = np.zeros_like(v)
+        N.check(self._lib.pfg_ilu_apply(self._h, N.ptr(v), N.ptr(out)))
+        return out
+
+    def resetILU(self):
+        """Drop the kept ILU(0) factor (the next ILU solve factors again)."""
+        N.check(self._lib.pfg_ilu_reset(self._h))
 
     def eliminate(self):
         """Apply the Dirichlet elimination of FEMSolver_%solve (FEMSolverClass.f90:1707-1756)
@@ -306,10 +338,12 @@ class FEMSolver:
         return lam, (None if X is None else X.T)
 
     def solve_device(self, b, x, algorithm="CG", preconditioning="BlockJacobi", precision="mixed",
-                     stop_rule=None, stream=None, update_mode=0, reliable_delta=None, storage="full"):
+                     stop_rule=None, stream=None, update_mode=0, reliable_delta=None, storage="full",
+                     ilu_order="stored"):
         """Solve with the already-eliminated matrix on device tensors b -> x
         (x holds x0).  ``b`` and ``x`` are float64 CUDA tensors."""
-        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, reliable_delta, storage)
+        opts = self._opts(algorithm, precision, preconditioning, stop_rule, update_mode, reliable_delta, storage,
+                          ilu_order)
         info = N.Info()
         if stream is None:
             _torch_sync()  # the library works on its own stream: order after the caller's writes
