@@ -335,6 +335,73 @@ def modal_lines(n=60, nev=20, block=24, tol=1e-8):
     return out
 
 
+def ilu_lines(n_solve=20, n_sweep=(60, 100), tol=1e-10):
+    """ILU(0)-preconditioned BiCGSTAB (FEMSolver_%solve(preconditioning="ILU") ->
+    bicgstab_CRS_ILU): factor in ascending column order, D^-1 L^-1 sweeps, FP64,
+    to a 1e-10 true relative residual, on the n_solve^3 lognormal cube (the
+    reference's CPU-runnable size), beside FP64 block-Jacobi BiCGSTAB and the
+    oracle's CPU restatement of the same ILU solve.  Factor and sweep times
+    alone on the larger cubes (the D^-1 L^-1 operator leaves BiCGSTAB diverging
+    on the 100^3 system, so no solve there)."""
+    import ctypes as C
+    import torch
+    from plantfem_gb300 import FEMSolver, problems
+    from plantfem_gb300 import _native as N
+
+    def system(n):
+        p = problems.lognormal(n)
+        s = FEMSolver()
+        s.setDomain(p["domain"])
+        s.setCRS(3)
+        s.assembleStiffness(p["E"], p["nu"])
+        s.setRHS(p["rhs"])
+        s.fix(1, p["fix_ids"], FixValue=0.0)
+        s.relative_er, s.er0, s.itrmax = tol, 1e-30, 20000
+        s.eliminate()
+        return s
+
+    def factor_and_sweep(s):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        N.check(s._lib.pfg_ilu_factor(s._h, 1, None))
+        f_ms = (time.perf_counter() - t) * 1e3
+        ms, by = C.c_double(), C.c_double()
+        N.check(s._lib.pfg_profile_kernel(s._h, 9, 20, C.byref(ms), C.byref(by)))
+        return {"factor_ms": round(f_ms, 2), "sweep_ms": round(ms.value, 4),
+                "sweep_bytes": by.value, "sweep_GBs": round(by.value / ms.value / 1e6, 1)}
+
+    out = {}
+    s = system(n_solve)
+    row = {"dof": s.ndof()}
+    row.update(factor_and_sweep(s))
+    b = torch.tensor(s.CRS_RHS, dtype=torch.float64, device="cuda")
+    x = torch.zeros_like(b)
+    for tag, pc, kw in (("ilu", "ILU", {"ilu_order": "sorted"}), ("block_jacobi", "BlockJacobi", {})):
+        for _ in range(2):  # the first run captures the graphs
+            x.zero_()
+            i = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=pc, precision="fp64",
+                               stop_rule="true_relative", **kw)
+        row[tag] = {"ms": round(i["solve_ms"], 2), "iterations": i["iterations"],
+                    "rel_residual": i["rel_residual"], "status": i["status"], "kernel_launches": i["kernel_launches"]}
+    # the same ILU solve by the oracle on the host cores (factor + solve)
+    import oracle as O
+    rp, ci, val = s.getCRS()
+    bh = np.array(s.CRS_RHS)
+    t = time.perf_counter()
+    lu = O.ilu0(rp, ci, val, sorted=True)
+    xo, rc, it = O.bicgstab_ilu(rp, ci, val, bh, lu=lu, er0=1e-30, relative_er=tol)
+    row["cpu_oracle"] = {"ms": round((time.perf_counter() - t) * 1e3, 1), "iterations": it, "rc": rc,
+                         "threads": O.num_threads(), "note": "ILU factor serial, SpMV OpenMP rows, sweeps serial"}
+    row["rel_diff_gpu_vs_oracle"] = float(np.linalg.norm(x.cpu().numpy() - xo) / np.linalg.norm(xo))
+    out[f"lognormal{n_solve}"] = row
+    s.remove()
+    for n in n_sweep:
+        s = system(n)
+        out[f"lognormal{n}_factor_sweep"] = dict({"dof": s.ndof()}, **factor_and_sweep(s))
+        s.remove()
+    return out
+
+
 def newmark_lines(n=60, steps=40, dt=1e-3):
     """Linear Newmark-beta time stepping (SeismicAnalysis_%LinearReyleighNewmark):
     the n^3 cantilever of the modal workload (x = 0 clamped, rho 1e3, E 1e4,
@@ -577,6 +644,12 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
             out_extra["newmark"] = newmark_lines()
         except Exception as e:
             out_extra["newmark"] = {"error": str(e)}
+    if not args.skip_ilu and rank == 0:
+        try:
+            out_extra["ilu_bicgstab"] = ilu_lines()
+        except Exception as e:
+            out_extra["ilu_bicgstab"] = {"error": str(e)}
+        _progress("ILU lines done")
     if not args.skip_batch and rank == 0:
         try:
             out_extra["batched_slabs"] = batch_lines(args.batch_count)
@@ -721,6 +794,7 @@ def main():
     ap.add_argument("--batch-count", type=int, default=512, help="slabs in the batched solve lines")
     ap.add_argument("--skip-adjoint", action="store_true", help="skip the 64^3 adjoint lines")
     ap.add_argument("--skip-newmark", action="store_true", help="skip the Newmark-beta time-stepping lines")
+    ap.add_argument("--skip-ilu", action="store_true", help="skip the ILU(0)-preconditioned BiCGSTAB lines")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
