@@ -109,6 +109,89 @@ class FEMDomain:
             f.write("\n".join(lines) + "\n")
         return path
 
+    # nodes per cell of the VTK cell types ImportVTKFileFEMDomain knows
+    # (FEMDomainClass.f90:13388-13421)
+    _VTK_NODES = {1: 1, 2: 1, 3: 2, 5: 3, 8: 4, 9: 4, 10: 4, 11: 8, 12: 8, 13: 6, 21: 3, 22: 6, 23: 8, 24: 10,
+                  25: 16}
+
+    def importVTKFile(self, name: str) -> "FEMDomain":
+        """FEMDomain_%importVTKFile (ImportVTKFileFEMDomain, FEMDomainClass.f90:13254 onwards):
+        read a legacy ASCII VTK unstructured grid: POINTS into nodcoord, CELLS
+        (0-based in the file) into 1-based elemnod, keeping only the cells of
+        the largest CELL_TYPES value when types are mixed (as the reference),
+        and POINT_DATA / CELL_DATA SCALARS, VECTORS and TENSORS into
+        ``PhysicalField`` (a list of {"name", "scalar" | "vector" | "tensor"}).
+        Values are read as whitespace-separated tokens, so files with several
+        points per line load too, and VECTORS / TENSORS are read without a
+        LOOKUP_TABLE line (the legacy format has none for them; the reference
+        skips one line there)."""
+        path = name if name.lower().endswith(".vtk") else name + ".vtk"
+        with open(path) as f:
+            raw = [ln.strip() for ln in f]
+        header = [ln for ln in raw[:4]]
+        if not any("ASCII" in ln for ln in header):
+            raise ValueError("importVTKFile: the VTK file must be ASCII")
+        if not any(ln.startswith("DATASET") and "UNSTRUCTURED_GRID" in ln for ln in raw[:6]):
+            raise ValueError("importVTKFile: DATASET must be UNSTRUCTURED_GRID")
+        lines = [ln for ln in raw[4:] if ln and not ln.startswith("#")]
+        pos = 0
+
+        def tokens(count):
+            nonlocal pos
+            out = []
+            while len(out) < count:
+                out += lines[pos].split()
+                pos += 1
+            return out
+
+        cells = types = None
+        data_count = 0
+        self.PhysicalField = []
+        nodcoord = None
+        while pos < len(lines):
+            head = lines[pos].split()
+            pos += 1
+            key = head[0].upper()
+            if key == "POINTS":
+                n = int(head[1])
+                nodcoord = np.array(tokens(3 * n), dtype=np.float64).reshape(n, 3)
+            elif key == "CELLS":
+                n, m = int(head[1]), int(head[2])
+                flat = np.array(tokens(m), dtype=np.int64)
+                cells, k = [], 0
+                for _ in range(n):
+                    c = int(flat[k])
+                    cells.append(flat[k + 1:k + 1 + c] + 1)
+                    k += c + 1
+            elif key == "CELL_TYPES":
+                if cells is None:
+                    raise ValueError("importVTKFile: no CELLS before CELL_TYPES")
+                types = np.array(tokens(int(head[1])), dtype=np.int64)
+            elif key in ("POINT_DATA", "CELL_DATA"):
+                data_count = int(head[1])
+            elif key == "SCALARS":
+                ncomp = int(head[3]) if len(head) > 3 else 1
+                if lines[pos].upper().startswith("LOOKUP_TABLE"):
+                    pos += 1
+                v = np.array(tokens(data_count * ncomp), dtype=np.float64)
+                self.PhysicalField.append({"name": head[1], "scalar": v if ncomp == 1 else v.reshape(-1, ncomp)})
+            elif key == "VECTORS":
+                v = np.array(tokens(3 * data_count), dtype=np.float64).reshape(data_count, 3)
+                self.PhysicalField.append({"name": head[1], "vector": v})
+            elif key == "TENSORS":
+                v = np.array(tokens(9 * data_count), dtype=np.float64).reshape(data_count, 3, 3)
+                self.PhysicalField.append({"name": head[1], "tensor": v})
+        if nodcoord is None or cells is None or types is None:
+            raise ValueError("importVTKFile: POINTS, CELLS and CELL_TYPES are required")
+        keep = int(types.max())
+        nne = self._VTK_NODES.get(keep)
+        if nne is None:
+            raise ValueError(f"importVTKFile: unknown cell type {keep}")
+        sel = [c for c, t in zip(cells, types) if t == keep and c.shape[0] == nne]
+        self.nodcoord = nodcoord
+        self.elemnod = np.array(sel, dtype=np.int32).reshape(len(sel), nne)
+        return self
+
     def deform(self, disp) -> "FEMDomain":
         """nodcoord += reshape(disp, nn, nd) with plantFEM's row-major reshape
         (FEMDomainClass.f90:14482, ArrayClass.f90:5328-5344)."""

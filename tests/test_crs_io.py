@@ -34,3 +34,30 @@ def test_vtk_hex8_mesh_with_fields(tmp_path):
     assert txt[k + 1].split() == ["8"] + [str(int(c) - 1) for c in dom.elemnod[0]]
     assert f"CELL_DATA {dom.ne()}" in txt and f"POINT_DATA {dom.nn()}" in txt and "CELL_TYPES 2" in txt
     assert np.allclose(dom.nodcoord.max(axis=0), [1.0, 1.0, 1.0])  # domain unchanged
+
+
+def test_vtk_import_round_trip_and_mixed_cells(tmp_path):
+    """importVTKFile (ImportVTKFileFEMDomain, FEMDomainClass.f90:13254): a file
+    written by FEMDomain.vtk reads back to the same mesh and fields; with mixed
+    cell types only the cells of the largest type are kept."""
+    from plantfem_gb300 import FEMDomain
+    dom = FEMDomain().create("Cube3D", 3, 2, 2)
+    dom.nodcoord = dom.nodcoord + np.random.default_rng(0).uniform(-0.01, 0.01, dom.nodcoord.shape)
+    sc = np.linspace(0.0, 1.0, dom.ne())
+    ve = np.random.default_rng(1).standard_normal((dom.nn(), 3))
+    te = np.random.default_rng(2).standard_normal((dom.ne(), 3, 3))
+    dom.vtk(str(tmp_path / "rt"), scalar=sc, vector=ve)
+    back = FEMDomain().importVTKFile(str(tmp_path / "rt"))
+    assert np.array_equal(back.nodcoord, dom.nodcoord) and np.array_equal(back.elemnod, dom.elemnod)
+    assert np.array_equal(back.PhysicalField[0]["scalar"], sc)
+    assert np.array_equal(back.PhysicalField[1]["vector"], ve)
+    dom.vtk(str(tmp_path / "t"), tensor=te)
+    assert np.array_equal(FEMDomain().importVTKFile(str(tmp_path / "t.vtk")).PhysicalField[0]["tensor"], te)
+    # mixed cells, two points per line
+    txt = ["# vtk DataFile Version 2.0", "mixed", "ASCII", "DATASET UNSTRUCTURED_GRID", "POINTS 9 float",
+           "0 0 0 1 0 0", "1 1 0 0 1 0", "0 0 1 1 0 1", "1 1 1 0 1 1", "2 0 0",
+           "CELLS 2 14", "4 1 2 8 0", "8 0 1 2 3 4 5 6 7", "CELL_TYPES 2", "10", "12"]
+    (tmp_path / "mx.vtk").write_text("\n".join(txt) + "\n")
+    m = FEMDomain().importVTKFile(str(tmp_path / "mx.vtk"))
+    assert m.nn() == 9 and m.elemnod.tolist() == [[1, 2, 3, 4, 5, 6, 7, 8]]
+    assert np.array_equal(m.nodcoord[8], [2.0, 0.0, 0.0])

@@ -37,3 +37,24 @@ def test_save_read_solve_and_load(cuda, tmp_path):
     s.loadMatrix("A")
     r3, c3, v3 = s.getCRS()
     assert np.array_equal(r3, rp) and np.array_equal(c3, ci) and np.array_equal(v3, v)
+
+
+def test_vtk_mesh_in_solves_like_the_original(cuda, tmp_path):
+    """A mesh written by FEMDomain.vtk and read back by importVTKFile assembles
+    and solves to the same displacement as the domain it came from."""
+    from plantfem_gb300 import FEMDomain
+    p = problems.lognormal(5, seed=4)
+    dom = p["domain"]
+    dom.vtk(str(tmp_path / "organ"))
+    back = FEMDomain().importVTKFile(str(tmp_path / "organ.vtk"))
+    xs = []
+    for d in (dom, back):
+        s = FEMSolver()
+        s.setDomain(d)
+        s.setCRS(3)
+        s.assembleStiffness(p["E"], p["nu"])
+        s.setRHS(p["rhs"])
+        s.fix(1, p["fix_ids"], FixValue=0.0)
+        s.relative_er = 1e-12
+        xs.append(s.solve(algorithm="CG", preconditioning="BlockJacobi", stop_rule="true_relative"))
+    assert np.array_equal(xs[0], xs[1])
