@@ -377,10 +377,11 @@ def ilu_lines(n_solve=20, n_sweep=(60, 100), tol=1e-10):
     b = torch.tensor(s.CRS_RHS, dtype=torch.float64, device="cuda")
     x = torch.zeros_like(b)
     for tag, pc, kw in (("ilu", "ILU", {"ilu_order": "sorted"}), ("block_jacobi", "BlockJacobi", {})):
-        for _ in range(2):  # the first run captures the graphs
-            x.zero_()
-            i = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=pc, precision="fp64",
-                               stop_rule="true_relative", **kw)
+        with _nvtx(f"{tag}_solve_{n_solve}"):  # profiler filter (ncu --nvtx-include)
+            for _ in range(2):  # the first run captures the graphs
+                x.zero_()
+                i = s.solve_device(b, x, algorithm="BiCGSTAB", preconditioning=pc, precision="fp64",
+                                   stop_rule="true_relative", **kw)
         row[tag] = {"ms": round(i["solve_ms"], 2), "iterations": i["iterations"],
                     "rel_residual": i["rel_residual"], "status": i["status"], "kernel_launches": i["kernel_launches"]}
     # the same ILU solve by the oracle on the host cores (factor + solve)
@@ -397,9 +398,33 @@ def ilu_lines(n_solve=20, n_sweep=(60, 100), tol=1e-10):
     s.remove()
     for n in n_sweep:
         s = system(n)
-        out[f"lognormal{n}_factor_sweep"] = dict({"dof": s.ndof()}, **factor_and_sweep(s))
+        with _nvtx(f"ilu_sweep_{n}"):
+            out[f"lognormal{n}_factor_sweep"] = dict({"dof": s.ndof()}, **factor_and_sweep(s))
         s.remove()
     return out
+
+
+class _nvtx:
+    """NVTX range around a bench section, so that a profiler can select it
+    (no effect without one)."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        try:
+            import torch
+            torch.cuda.nvtx.range_push(self.name)
+            self.on = True
+        except Exception:
+            self.on = False
+        return self
+
+    def __exit__(self, *exc):
+        if self.on:
+            import torch
+            torch.cuda.nvtx.range_pop()
+        return False
 
 
 def newmark_lines(n=60, steps=40, dt=1e-3):

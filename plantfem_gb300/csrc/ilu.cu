@@ -145,73 +145,130 @@ __global__ void __launch_bounds__(32 * kIluWarps)
         udiag[(int64_t)BS * I + lane] = pdiag >= 0 ? sm.rowv[(lane * BS + lane) * nbI + sm.seq[pdiag]] : 0.0;
 }
 
-// ILU_matvecCRS (SparseClass.f90:1795-1852) as executed, for the block rows
-// of one level: t_i = v_i - sum_{k<i} L(i,k) t_k, out_i = t_i / U(i,i) (1 for
-// a zero U(i,i)).  The lanes sum the blocks J < I, lane 0 finishes the BS
-// rows through the diagonal block's strictly lower part.
-//
-// Small levels run as a chain of programmatically dependent launches: a
-// level's grid is scheduled once every CTA of the level before it is past its
-// own wait, loads what does not depend on that level (its rows, block columns
-// and factor entries) and waits (griddepcontrol.wait: the previous grid
-// complete and its writes visible) only before it reads v and t.  t is read
-// through L2 (ld.global.cg).  Large levels launch plainly (the wait is then a
-// no-op): measured on GB300, early launch cut a 60^3 sweep (levels of <= ~900
-// block rows) from 3.87 to 2.85 ms but slowed the 100^3 one (levels of up to
-// ~2500) from 8.66 to 9.47 ms.
+// Sweep layout, built once per factor: the rows in level order, each with
+// its blocks J < I (block columns, and values transposed within the row as in
+// the matrix: entry (r, c) of block b at val[BB*off + (r*BS + c)*m + b]), and
+// per row the strictly lower part of its diagonal block and 1 / U(i,i) (1 for
+// a zero U(i,i), as ILU_matvecCRS reads it).  Each row then needs one load of
+// its (I, m, off) before its values, instead of order -> row pointer ->
+// block columns -> values.
+template <int BS>
+constexpr int diag_stride() { return BS == 3 ? 8 : 1; }  // [l10 l20 l21 r0 r1 r2 - -] or [r0]
+
 template <int BS>
 __global__ void __launch_bounds__(32 * kIluWarps)
-    k_ilu_lower(const int64_t *__restrict__ rp, const int *__restrict__ col, const double *__restrict__ lu,
-                const double *__restrict__ udiag, const int *__restrict__ order, int64_t start, int count,
+    k_ilu_sweep_layout(const int64_t *__restrict__ rp, const int *__restrict__ col, const double *__restrict__ lu,
+                       const double *__restrict__ udiag, const int *__restrict__ order,
+                       const int64_t *__restrict__ sw_off, int64_t nb, int2 *__restrict__ sw_row,
+                       int *__restrict__ sw_col, double *__restrict__ sw_val, double *__restrict__ sw_diag)
+{
+    constexpr int BB = BS * BS, SD = diag_stride<BS>();
+    const int lane = threadIdx.x & 31;
+    const int64_t p = (int64_t)blockIdx.x * kIluWarps + (threadIdx.x >> 5);
+    if (p >= nb) return;
+    const int I = order[p];
+    const int64_t base = rp[I];
+    const int nbI = (int)(rp[I + 1] - base);
+    const int64_t off = sw_off[p];
+    const int m = (int)(sw_off[p + 1] - off);
+    if (lane == 0) sw_row[p] = make_int2(I, m);
+    int carry = 0;
+    for (int b0 = 0; b0 < nbI; b0 += 32) {
+        const int b = b0 + lane;
+        const int J = b < nbI ? col[base + b] : INT_MAX;
+        const unsigned low = __ballot_sync(0xffffffffu, J < I);
+        if (J < I) {
+            const int r = carry + __popc(low & ((1u << lane) - 1u));
+            sw_col[off + r] = J;
+#pragma unroll
+            for (int rc = 0; rc < BB; ++rc) sw_val[BB * off + (int64_t)rc * m + r] = lu[BB * base + (int64_t)rc * nbI + b];
+        } else if (J == I && BS == 3) {
+            sw_diag[SD * p + 0] = lu[BB * base + (int64_t)(1 * BS + 0) * nbI + b];
+            sw_diag[SD * p + 1] = lu[BB * base + (int64_t)(2 * BS + 0) * nbI + b];
+            sw_diag[SD * p + 2] = lu[BB * base + (int64_t)(2 * BS + 1) * nbI + b];
+        }
+        carry += __popc(low);
+    }
+    if (lane < BS) {
+        const double d = udiag[(int64_t)BS * I + lane];
+        sw_diag[SD * p + (BS == 3 ? 3 : 0) + lane] = d == 0.0 ? 1.0 : 1.0 / d;
+    }
+}
+
+// Lanes per block row in the sweep, and block slots a lane loads before the
+// wait (rows with more than kSweepLanes * kSweepSlots blocks J < I load the
+// rest after it).  GB300 runs a warp-wide FP64 instruction in 16 cycles of
+// its SM's FP64 pipe, which the widest levels saturate: eight lanes per row
+// (a structured hex mesh has 13 blocks J < I per row) keep most lanes of
+// every FP64 instruction busy and cut the reduction to three rounds.
+constexpr int kSweepLanes = 8;
+constexpr int kSweepSlots = 2;
+constexpr int kSweepRows = kIluWarps * 32 / kSweepLanes;  // block rows per CTA
+
+// ILU_matvecCRS (SparseClass.f90:1795-1852) as executed, for the block rows
+// of one level: t_i = v_i - sum_{k<i} L(i,k) t_k, out_i = t_i / U(i,i) (taken
+// as 1 for a zero U(i,i)).  kSweepLanes lanes sum a row's blocks J < I, the
+// first of them finishes the BS rows through the diagonal block's strictly
+// lower part.
+//
+// Levels after the first of at most kIluEarlyRows block rows run as
+// programmatically dependent grids: a level's grid is scheduled once every CTA
+// of the level before it is past its own wait, loads what does not depend on
+// that level (its row, block columns, factor values, v) and waits
+// (griddepcontrol.wait: the previous grid complete, its writes visible) only
+// before it reads t, through L2 (ld.global.cg).  The first level launches
+// plainly, after the pass that wrote v.  Larger levels launch plainly too (the
+// wait is then a no-op): early launch slowed the widest levels of a 100^3
+// sweep (up to ~2500 block rows) in measurement.
+template <int BS>
+__global__ void __launch_bounds__(32 * kIluWarps)
+    k_ilu_lower(const int2 *__restrict__ sw_row, const int64_t *__restrict__ sw_off, const int *__restrict__ sw_col,
+                const double *__restrict__ sw_val, const double *__restrict__ sw_diag, int64_t start, int count,
                 const double *v, double *t, double *out, const KState *S)
 {
-    constexpr int BB = BS * BS;
-    constexpr int NS = kIluMaxBlocks / 32;  // block slots per lane
-    const int lane = threadIdx.x & 31;
-    const int idx = blockIdx.x * kIluWarps + (threadIdx.x >> 5);
-    const bool active = idx < count;  // the same for the whole warp
-    int I = 0, bd = -1;
-    int J[NS];
-    double gv[NS][BB];
-    double ld[BS > 1 ? BS * BS : 1], dg[BS];
+    constexpr int BB = BS * BS, SD = diag_stride<BS>();
+    const int sub = threadIdx.x % kSweepLanes;
+    const int idx = blockIdx.x * kSweepRows + threadIdx.x / kSweepLanes;
+    const bool active = idx < count;  // the same for the row's lanes
+    int I = 0, m = 0;
+    int64_t off = 0;
+    int J[kSweepSlots];
+    double gv[kSweepSlots][BB];
+    double dd[SD], vI[BS];
+#pragma unroll
+    for (int q = 0; q < kSweepSlots; ++q) J[q] = -1;
     if (active) {
-        I = order[start + idx];
-        const int64_t base = rp[I];
-        const int nbI = (int)(rp[I + 1] - base);
-        const double *g = lu + BB * base;
+        const int64_t p = start + idx;
+        const int2 rm = sw_row[p];
+        off = sw_off[p];
+        I = rm.x;
+        m = rm.y;
 #pragma unroll
-        for (int q = 0; q < NS; ++q) {
-            const int b = lane + 32 * q;
-            J[q] = b < nbI ? col[base + b] : INT_MAX;
-            if (J[q] < I) {
+        for (int q = 0; q < kSweepSlots; ++q) {
+            const int b = sub + kSweepLanes * q;
+            if (b < m) {
+                J[q] = sw_col[off + b];
 #pragma unroll
-                for (int rc = 0; rc < BB; ++rc) gv[q][rc] = g[rc * nbI + b];
-            } else if (J[q] == I) {
-                bd = b;
+                for (int rc = 0; rc < BB; ++rc) gv[q][rc] = sw_val[BB * off + (int64_t)rc * m + b];
             }
         }
+        if (sub == 0) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) bd = max(bd, __shfl_xor_sync(0xffffffffu, bd, o));
-        if (lane == 0) {
+            for (int k = 0; k < SD; ++k) dd[k] = sw_diag[SD * p + k];
 #pragma unroll
-            for (int d = 0; d < BS; ++d) {
-                dg[d] = udiag[(int64_t)BS * I + d];
-#pragma unroll
-                for (int e = 0; e < d; ++e) ld[d * BS + e] = bd >= 0 ? g[(d * BS + e) * nbI + bd] : 0.0;
-            }
+            for (int d = 0; d < BS; ++d) vI[d] = __ldcg(v + (int64_t)BS * I + d);
         }
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     // only now may the next level's grid be scheduled: one level ahead at most
     asm volatile("griddepcontrol.launch_dependents;");
-    if (!active) return;
-    if (S != nullptr && (S->done | S->need_update)) return;
+    if (S != nullptr && (S->done | S->need_update)) return;  // the same for the whole grid
     double acc[BS];
 #pragma unroll
     for (int d = 0; d < BS; ++d) acc[d] = 0.0;
 #pragma unroll
-    for (int q = 0; q < NS; ++q) {
-        if (J[q] < I) {
+    for (int q = 0; q < kSweepSlots; ++q) {
+        if (J[q] >= 0) {
             double tj[BS];
 #pragma unroll
             for (int e = 0; e < BS; ++e) tj[e] = __ldcg(t + (int64_t)BS * J[q] + e);
@@ -221,21 +278,39 @@ __global__ void __launch_bounds__(32 * kIluWarps)
                 for (int e = 0; e < BS; ++e) acc[d] = fma(gv[q][d * BS + e], tj[e], acc[d]);
         }
     }
+    for (int b = sub + kSweepLanes * kSweepSlots; b < m; b += kSweepLanes) {
+        const int Jb = sw_col[off + b];
+        double tj[BS];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+        for (int e = 0; e < BS; ++e) tj[e] = __ldcg(t + (int64_t)BS * Jb + e);
+#pragma unroll
+        for (int d = 0; d < BS; ++d)
+#pragma unroll
+            for (int e = 0; e < BS; ++e)
+                acc[d] = fma(sw_val[BB * off + (int64_t)(d * BS + e) * m + b], tj[e], acc[d]);
+    }
+    // every lane takes part (inactive rows add zeros): xor partners stay in the row's lanes
+#pragma unroll
+    for (int o = kSweepLanes / 2; o > 0; o >>= 1) {
 #pragma unroll
         for (int d = 0; d < BS; ++d) acc[d] += __shfl_xor_sync(0xffffffffu, acc[d], o);
     }
-    if (lane == 0) {
-        double tv[BS];
-#pragma unroll
-        for (int d = 0; d < BS; ++d) {
-            double s = __ldcg(v + (int64_t)BS * I + d) - acc[d];
-#pragma unroll
-            for (int e = 0; e < d; ++e) s -= ld[d * BS + e] * tv[e];
-            tv[d] = s;
-            t[(int64_t)BS * I + d] = s;
-            out[(int64_t)BS * I + d] = s / (dg[d] == 0.0 ? 1.0 : dg[d]);
+    if (active && sub == 0) {
+        if constexpr (BS == 3) {
+            const double t0 = vI[0] - acc[0];
+            const double t1 = vI[1] - acc[1] - dd[0] * t0;
+            const double t2 = vI[2] - acc[2] - dd[1] * t0 - dd[2] * t1;
+            double *tr = t + (int64_t)3 * I, *orow = out + (int64_t)3 * I;
+            tr[0] = t0;
+            tr[1] = t1;
+            tr[2] = t2;
+            orow[0] = t0 * dd[3];
+            orow[1] = t1 * dd[4];
+            orow[2] = t2 * dd[5];
+        } else {
+            const double t0 = vI[0] - acc[0];
+            t[I] = t0;
+            out[I] = t0 * dd[0];
         }
     }
 }
@@ -243,11 +318,12 @@ __global__ void __launch_bounds__(32 * kIluWarps)
 // Levels of at most this many block rows launch early (see k_ilu_lower).
 constexpr int kIluEarlyRows = 1024;
 
-// One level of the sweep on st, programmatically dependent when it is small.
+// One level of the sweep on st, programmatically dependent when it is not
+// the first and is small.
 template <int BS>
-void launch_lower(int grid, const int64_t *rp, const int *col, const double *lu, const double *udiag,
-                  const int *order, int64_t start, int count, const double *v, double *t, double *out,
-                  const KState *S, cudaStream_t st)
+void launch_lower(int grid, bool early, const int2 *sw_row, const int64_t *sw_off, const int *sw_col,
+                  const double *sw_val, const double *sw_diag, int64_t start, int count, const double *v, double *t,
+                  double *out, const KState *S, cudaStream_t st)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -258,8 +334,9 @@ void launch_lower(int grid, const int64_t *rp, const int *col, const double *lu,
     at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
-    cfg.numAttrs = count <= kIluEarlyRows ? 1 : 0;
-    PFG_CUDA(cudaLaunchKernelEx(&cfg, k_ilu_lower<BS>, rp, col, lu, udiag, order, start, count, v, t, out, S));
+    cfg.numAttrs = early ? 1 : 0;
+    PFG_CUDA(cudaLaunchKernelEx(&cfg, k_ilu_lower<BS>, sw_row, sw_off, sw_col, sw_val, sw_diag, start, count, v, t,
+                                out, S));
 }
 
 int ilu_grid(int64_t count) { return (int)((count + kIluWarps - 1) / kIluWarps); }
@@ -281,15 +358,12 @@ void Ilu0::factor(const DevMatrix &A, bool sorted, cudaStream_t st)
     PFG_CUDA(cudaStreamSynchronize(st));
     std::vector<int> lvl((size_t)A.nb);
     int nl = 0;
-    int64_t lower = 0;
     for (int64_t I = 0; I < A.nb; ++I) {
         PFG_CHECK(rp[I + 1] - rp[I] <= kIluMaxBlocks, PFG_E_UNSUPPORTED,
                   "ILU(0): a row stores more than 64 blocks");
         int L = 0;
-        for (int64_t q = rp[I]; q < rp[I + 1]; ++q) {
+        for (int64_t q = rp[I]; q < rp[I + 1]; ++q)
             if (col[q] < I) L = std::max(L, lvl[col[q]] + 1);
-            lower += col[q] <= I;
-        }
         lvl[I] = L;
         nl = std::max(nl, L + 1);
     }
@@ -302,7 +376,6 @@ void Ilu0::factor(const DevMatrix &A, bool sorted, cudaStream_t st)
         for (int64_t I = 0; I < A.nb; ++I) order[(size_t)fill[lvl[I]]++] = (int)I;
     }
     const int64_t n = A.ndof();
-    sweep_bytes_ = (double)lower * (A.bs * A.bs * 8.0 + 4.0) + (double)A.nb * (8.0 + 4.0) + 5.0 * (double)n * 8.0;
     order_.resize((size_t)A.nb);
     lu_.resize(A.v64.n);
     udiag_.resize((size_t)n);
@@ -320,7 +393,35 @@ void Ilu0::factor(const DevMatrix &A, bool sorted, cudaStream_t st)
                                                                      lptr_[L], (int)cnt, sorted ? 1 : 0);
     }
     PFG_CUDA(cudaGetLastError());
+    // the sweep layout: rows in level order with their blocks J < I
+    std::vector<int64_t> off((size_t)A.nb + 1, 0);
+    for (int64_t q = 0; q < A.nb; ++q) {
+        const int I = order[(size_t)q];
+        int m = 0;
+        for (int64_t k = rp[I]; k < rp[I + 1]; ++k) m += col[k] < I;
+        off[(size_t)q + 1] = off[(size_t)q] + m;
+    }
+    const int64_t nlow = off[(size_t)A.nb];
+    sw_off_.resize((size_t)A.nb + 1);
+    sw_row_.resize((size_t)A.nb);
+    sw_col_.resize((size_t)std::max<int64_t>(nlow, 1));
+    sw_val_.resize((size_t)std::max<int64_t>(nlow * A.bs * A.bs, 1));
+    sw_diag_.resize((size_t)A.nb * (A.bs == 3 ? 8 : 1));
+    PFG_CUDA(cudaMemcpyAsync(sw_off_.p, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    // a row without a stored diagonal block keeps zero lower entries there
+    PFG_CUDA(cudaMemsetAsync(sw_diag_.p, 0, sw_diag_.bytes(), st));
+    if (A.bs == 3)
+        k_ilu_sweep_layout<3><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(A.rp.p, A.col.p, lu_.p, udiag_.p, order_.p,
+                                                                        sw_off_.p, A.nb, sw_row_.p, sw_col_.p,
+                                                                        sw_val_.p, sw_diag_.p);
+    else
+        k_ilu_sweep_layout<1><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(A.rp.p, A.col.p, lu_.p, udiag_.p, order_.p,
+                                                                        sw_off_.p, A.nb, sw_row_.p, sw_col_.p,
+                                                                        sw_val_.p, sw_diag_.p);
+    PFG_CUDA(cudaGetLastError());
     PFG_CUDA(cudaStreamSynchronize(st));
+    sweep_bytes_ = (double)nlow * (A.bs * A.bs * 8.0 + 4.0) +
+                   (double)A.nb * (8.0 + 8.0 + 8.0 * (A.bs == 3 ? 8 : 1)) + 4.0 * (double)n * 8.0;
     bs_ = A.bs;
     nb_ = A.nb;
     nnzb_ = A.nnzb;
@@ -338,12 +439,14 @@ int Ilu0::apply(const double *v, double *out, const KState *S, cudaStream_t st) 
     const int nl = levels();
     for (int L = 0; L < nl; ++L) {
         const int64_t cnt = lptr_[L + 1] - lptr_[L];
+        const bool early = L > 0 && cnt <= kIluEarlyRows;
+        const int grid = (int)((cnt + kSweepRows - 1) / kSweepRows);
         if (bs_ == 3)
-            launch_lower<3>(ilu_grid(cnt), rp_, col_, lu_.p, udiag_.p, order_.p, lptr_[L], (int)cnt, v, t_.p, out, S,
-                            st);
+            launch_lower<3>(grid, early, sw_row_.p, sw_off_.p, sw_col_.p, sw_val_.p, sw_diag_.p, lptr_[L],
+                            (int)cnt, v, t_.p, out, S, st);
         else
-            launch_lower<1>(ilu_grid(cnt), rp_, col_, lu_.p, udiag_.p, order_.p, lptr_[L], (int)cnt, v, t_.p, out, S,
-                            st);
+            launch_lower<1>(grid, early, sw_row_.p, sw_off_.p, sw_col_.p, sw_val_.p, sw_diag_.p, lptr_[L],
+                            (int)cnt, v, t_.p, out, S, st);
     }
     PFG_CUDA(cudaGetLastError());
     return nl;

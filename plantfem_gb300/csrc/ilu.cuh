@@ -49,9 +49,9 @@ class Ilu0 {
     // Factor values in the matrix's block-row layout and the U diagonal.
     const double *lu() const { return lu_.p; }
     const double *udiag() const { return udiag_.p; }
-    // Algorithmic bytes of one apply: the stored blocks with J <= I (values
-    // and block columns), row pointers and level order, v, t written and
-    // gathered once, U's diagonal, out.
+    // Algorithmic bytes of one apply: the blocks J < I (values and block
+    // columns) and the per-row entries of the sweep layout once, v, t
+    // written and gathered once, out.
     double sweep_bytes() const { return sweep_bytes_; }
 
   private:
@@ -64,6 +64,13 @@ class Ilu0 {
     const int *col_ = nullptr;
     DevBuf<double> lu_, udiag_, t_;
     DevBuf<int> order_;           // block rows grouped by level, ascending within a level
+    // sweep layout (ilu.cu): per level-ordered row (I, number of blocks J < I),
+    // offset of its blocks, their block columns and values, diagonal-block
+    // lower part and 1 / U(i,i)
+    DevBuf<int2> sw_row_;
+    DevBuf<int64_t> sw_off_;
+    DevBuf<int> sw_col_;
+    DevBuf<double> sw_val_, sw_diag_;
     std::vector<int64_t> lptr_;   // level L holds order_[lptr_[L] .. lptr_[L+1])
 };
 
