@@ -1129,6 +1129,7 @@ int pfg_newmark_step(pfg_solver *h, const pfg_solve_opts *opts, int64_t n, const
             cfg.algorithm = PFG_ALG_CG;
             cfg.precond = PFG_PC_BLOCK_JACOBI;
             cfg.stop_rule = PFG_STOP_TRUE_RELATIVE;
+            cfg.graph_chunk = 8;  // short warm-started solves
         }
         res = h->kry.solve(h->K, nm.rhs.p, nm.x.p, cfg, h->st);
         if (h->have_fix) restore_fixed(n, nm.x.p, h->fixed_d.p, h->fixval_d.p, h->st);

@@ -1569,11 +1569,15 @@ SolveResult Krylov::run_cg64(DevMatrix &A, const double *b, double *x, const KCo
         graph_key_ = key;
         graph_kernels_ = nk;
     }
+    bool fresh = false;  // res.rel_residual is the true residual of the current x
     for (int restart = 0; restart < 20; ++restart) {
         // r = b - A x (true residual), restart the recurrences from it
         double rel = true_residual(A, b, x, r_.p, st);
         res.rel_residual = rel;
-        if (rel <= cfg.relative_er) break;
+        if (rel <= cfg.relative_er) {
+            fresh = true;
+            break;
+        }
         PFG_CUDA(cudaMemsetAsync(pA_.p, 0, n * sizeof(double), st));
         PFG_CUDA(cudaMemsetAsync(pB_.p, 0, n * sizeof(double), st));
         if (A.bs == 3)
@@ -1603,7 +1607,7 @@ SolveResult Krylov::run_cg64(DevMatrix &A, const double *b, double *x, const KCo
         int zero = 0;
         PFG_CUDA(cudaMemcpyAsync(&state_.p->done, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     }
-    res.rel_residual = true_residual(A, b, x, r_.p, st);
+    if (!fresh) res.rel_residual = true_residual(A, b, x, r_.p, st);
     if (res.rel_residual > cfg.relative_er && res.status == PFG_OK) res.status = PFG_W_NOT_CONVERGED;
     return res;
 }
@@ -1656,12 +1660,15 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
         graph_kernels_ = nk;
     }
     const int max_restarts = cfg.stop_rule == PFG_STOP_REFERENCE ? 1 : 20;
+    bool fresh = false;  // res.rel_residual is the true residual of the current x
     for (int restart = 0; restart < max_restarts; ++restart) {
         double rel = true_residual(A, b, x, r_.p, st);
         res.rel_residual = rel;
+        fresh = true;
         if (cfg.stop_rule == PFG_STOP_TRUE_RELATIVE && rel <= cfg.relative_er) break;
         // bicgstab_CRS_ILU returns before its loop when |r|^2 < er0 (:4150)
         if (ilu && cfg.stop_rule == PFG_STOP_REFERENCE && host_state_->true_rr < cfg.er0) break;
+        fresh = false;
         PFG_CUDA(cudaMemsetAsync(pA_.p, 0, n * sizeof(double), st));
         PFG_CUDA(cudaMemsetAsync(pB_.p, 0, n * sizeof(double), st));
         PFG_CUDA(cudaMemsetAsync(yA_.p, 0, n * sizeof(double), st));
@@ -1688,7 +1695,7 @@ SolveResult Krylov::run_bicgstab64(DevMatrix &A, const double *b, double *x, con
         int zero = 0;
         PFG_CUDA(cudaMemcpyAsync(&state_.p->done, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
     }
-    res.rel_residual = true_residual(A, b, x, r_.p, st);
+    if (!fresh) res.rel_residual = true_residual(A, b, x, r_.p, st);
     if (cfg.stop_rule == PFG_STOP_TRUE_RELATIVE && res.rel_residual > cfg.relative_er && res.status == PFG_OK)
         res.status = PFG_W_NOT_CONVERGED;
     return res;
