@@ -786,42 +786,59 @@ void restore_fixed(int64_t n, double *x, const uint8_t *fixed, const double *fix
 // ------------------------------------------------------------ CRS in / out
 // 3x3 node-block structure check: rows 3I..3I+2 have equal length L = 3*nblk
 // and row 3I+r holds [3c+1, 3c+2, 3c+3] for the same node sequence c.
+// A scalar CRS is taken as 3x3 blocks when every node row I has three scalar
+// rows 3I..3I+2 of equal length L (a multiple of 3), starting at a multiple of
+// 9 entries, and each group of three columns reads 3c+1, 3c+2, 3c+3 in all
+// three rows (the layout FEMDomainClass.f90:10780-10836 produces).  The three
+// rows of node row I are then one contiguous run of 3L entries.  One warp per
+// node row, lanes over the run (coalesced).
 __global__ void k_check_blocks(int64_t nb, const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
                                int64_t n, int *ok)
 {
-    for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < nb; I += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t I = w0; I < nb; I += nw) {
         const int64_t s0 = row_ptr[3 * I] - 1;
         const int64_t L = row_ptr[3 * I + 1] - row_ptr[3 * I];
         bool good = (L % 3) == 0 && (s0 % 9) == 0 && row_ptr[3 * I + 2] - row_ptr[3 * I + 1] == L &&
                     row_ptr[3 * I + 3] - row_ptr[3 * I + 2] == L;
-        for (int r = 0; r < 3 && good; ++r) {
-            const int64_t s = row_ptr[3 * I + r] - 1;
-            for (int64_t k = 0; k < L / 3 && good; ++k) {
+        if (good) {
+            for (int64_t t = lane; t < 3 * L; t += 32) {
+                const int64_t q = t % L, k = q / 3, cc = q % 3;
                 const int32_t c0 = col_idx[s0 + 3 * k];
-                if ((c0 - 1) % 3 != 0 || c0 < 1 || c0 > n) good = false;
-                for (int cc = 0; cc < 3 && good; ++cc)
-                    if (col_idx[s + 3 * k + cc] != c0 + cc) good = false;
+                if ((c0 - 1) % 3 != 0 || c0 < 1 || c0 > n || col_idx[s0 + t] != c0 + (int32_t)cc) good = false;
             }
         }
-        if (!good) *ok = 0;
+        if (__any_sync(0xffffffffu, !good) && lane == 0) *ok = 0;
     }
 }
 
+// Scalar CRS (checked by k_check_blocks) -> the block-row layout (bsr.cuh):
+// node row I's run of 9 nblk values, entry t = r (3 nblk) + 3k + c, lands at
+// bval[9 bs + (3r + c) nblk + k].  One warp per node row: coalesced reads,
+// writes inside the row's own 72 nblk bytes.
 __global__ void k_import_b3(int64_t nb, const int64_t *__restrict__ row_ptr, const int32_t *__restrict__ col_idx,
                             const double *__restrict__ val, int64_t *__restrict__ rp, int *__restrict__ bcol,
                             double *__restrict__ bval)
 {
-    for (int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; I < nb; I += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t I = w0; I < nb; I += nw) {
         const int64_t s0 = row_ptr[3 * I] - 1;
         const int nblk = (int)((row_ptr[3 * I + 1] - row_ptr[3 * I]) / 3);
         const int64_t bs = s0 / 9;
-        rp[I] = bs;
-        if (I == nb - 1) rp[nb] = bs + nblk;
-        for (int k = 0; k < nblk; ++k) bcol[bs + k] = (col_idx[s0 + 3 * k] - 1) / 3;
-        for (int r = 0; r < 3; ++r) {
-            const int64_t s = row_ptr[3 * I + r] - 1;
-            for (int k = 0; k < nblk; ++k)
-                for (int c = 0; c < 3; ++c) bval[bs * 9 + (int64_t)(3 * r + c) * nblk + k] = val[s + 3 * k + c];
+        if (lane == 0) {
+            rp[I] = bs;
+            if (I == nb - 1) rp[nb] = bs + nblk;
+        }
+        for (int k = lane; k < nblk; k += 32) bcol[bs + k] = (col_idx[s0 + 3 * k] - 1) / 3;
+        if (val == nullptr) continue;
+        const int run = 3 * nblk;
+        for (int t = lane; t < 3 * run; t += 32) {
+            const int r = t / run, q = t - r * run, k = q / 3, c = q - 3 * k;
+            bval[bs * 9 + (int64_t)(3 * r + c) * nblk + k] = val[s0 + t];
         }
     }
 }
