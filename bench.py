@@ -646,12 +646,15 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
         del rp, ci, val
         xn[:] = 0
         linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL, storage=STORAGE)  # warm-up: allocations, graphs
-        e2e_steps = max(1, min(args.steps, 3))
+        e2e_steps = max(1, min(args.steps, 5))
         t_a = time.perf_counter()
-        e2e_infos = []
-        for _ in range(e2e_steps):
-            xn[:] = 0
-            e2e_infos.append(linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL, storage=STORAGE))
+        e2e_infos, e2e_each = [], []
+        with _nvtx("e2e"):  # profiler filter (ncu --nvtx-include)
+            for _ in range(e2e_steps):
+                t_1 = time.perf_counter()
+                xn[:] = 0
+                e2e_infos.append(linear_solver_crs(rpn, cin, valn, rhsn, xn, relative_er=TOL, storage=STORAGE))
+                e2e_each.append(round((time.perf_counter() - t_1) * 1e3, 1))
         t_e2e = (time.perf_counter() - t_a) / e2e_steps
         h2d = rpn.nbytes + cin.nbytes + valn.nbytes + rhsn.nbytes + xn.nbytes
         # the same pinned arrays copied by torch alone: the host link's share
@@ -665,6 +668,7 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
         del dev
         e2e = {"value": round(ws / t_e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(xn.nbytes), "ms_per_step": round(t_e2e * 1e3, 2),
+               "ms_each": e2e_each,
                "solver_device_ms": round(float(np.mean([i["solve_ms"] for i in e2e_infos])), 2),
                "pinned_h2d_GBs": round((rpn.nbytes + cin.nbytes + valn.nbytes) / t_c / 1e9, 1),
                "path": "pfg_linear_solver_crs (FEMSolver_%solve LinearSolver hook) with pinned host CRS",

@@ -7,6 +7,7 @@
 // copied in at set*/fix and out at solve/eig/getCRS, like the reference's
 // value-semantics setters.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -609,6 +610,15 @@ int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const 
         }
         pfg_solver *h = ctx;
         std::lock_guard<std::mutex> lk(h->mu);
+        const KConfig cfg = to_config(opts);
+        // debug: host time of each phase (the stream is drained at each mark)
+        const auto t0 = std::chrono::steady_clock::now();
+        auto mark = [&](const char *what) {
+            if (cfg.debug == 0) return;
+            PFG_CUDA(cudaStreamSynchronize(h->st));
+            const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            fprintf(stderr, "[pfg] linear_solver_crs %-8s %9.3f ms\n", what, ms);
+        };
         static thread_local DevBuf<int64_t> rp;
         static thread_local DevBuf<int32_t> ci;
         static thread_local DevBuf<double> v, b;
@@ -620,16 +630,19 @@ int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const 
         PFG_CUDA(cudaMemcpyAsync(ci.p, col_idx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice, h->st));
         PFG_CUDA(cudaMemcpyAsync(v.p, val, nnz * sizeof(double), cudaMemcpyHostToDevice, h->st));
         PFG_CUDA(cudaMemcpyAsync(b.p, rhs, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        mark("copy-in");
         // same sizes as the previous call: the import reuses the device
         // buffers (same addresses), so the cached solver graphs stay valid
         import_crs(n, nnz, rp.p, ci.p, v.p, h->K, h->st);
         h->have_crs = true;
         h->x.ensure((size_t)n);
         PFG_CUDA(cudaMemcpyAsync(h->x.p, x, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-        const KConfig cfg = to_config(opts);
+        mark("import");
         res = h->kry.solve(h->K, b.p, h->x.p, cfg, h->st);
+        mark("solve");
         PFG_CUDA(cudaMemcpyAsync(x, h->x.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
         PFG_CUDA(cudaStreamSynchronize(h->st));
+        mark("copy-out");
         fill_info(info, res, cfg.precision);
     });
     if (rc != PFG_OK) return rc;

@@ -32,24 +32,46 @@ __global__ void k_sell_pattern(int64_t nb, int64_t ns, const int64_t *__restrict
     }
 }
 
+// Slice values, one warp per slice (lane = row of the slice), one entry plane
+// (r, c) and up to kTileK slots at a time through shared memory: each row's
+// plane is read as one contiguous run of its blocks (block row layout,
+// bsr.cuh) and written back slot by slot as 32 consecutive lanes.
+constexpr int kTileK = 64;
+constexpr int kTileWarps = 2;
+
 template <int BS, typename T>
-__global__ void k_sell_values(int64_t nb, int64_t ns, const int64_t *__restrict__ rp, const double *__restrict__ v64,
-                              const int64_t *__restrict__ sptr, T *__restrict__ sval)
+__global__ void __launch_bounds__(32 * kTileWarps)
+    k_sell_values(int64_t nb, int64_t ns, const int64_t *__restrict__ rp, const double *__restrict__ v64,
+                  const int64_t *__restrict__ sptr, T *__restrict__ sval)
 {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ns * 32; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = t >> 5;
-        const int l = (int)(t & 31);
-        const int64_t row = t;
-        const int64_t b0 = sptr[s], w = sptr[s + 1] - b0;
+    constexpr int BB = BS * BS;
+    __shared__ T tile[kTileWarps][32][kTileK + 1];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t s = (int64_t)blockIdx.x * kTileWarps + w; s < ns; s += (int64_t)gridDim.x * kTileWarps) {
+        const int64_t b0 = sptr[s];
+        const int wdt = (int)(sptr[s + 1] - b0);
+        const int64_t row = s * 32 + lane;
         const int64_t r0 = row < nb ? rp[row] : 0;
-        const int64_t nblk = row < nb ? rp[row + 1] - r0 : 0;
-        const double *src = v64 + r0 * (BS * BS);
-        for (int64_t k = 0; k < w; ++k)
-#pragma unroll
-            for (int e = 0; e < BS * BS; ++e)
-                sval[((b0 + k) * (BS * BS) + e) * 32 + l] = k < nblk ? (T)src[(int64_t)e * nblk + k] : T(0);
+        const int nblk = row < nb ? (int)(rp[row + 1] - r0) : 0;
+        for (int e = 0; e < BB; ++e)
+            for (int kc = 0; kc < wdt; kc += kTileK) {
+                for (int l = 0; l < 32; ++l) {
+                    const int64_t r0l = __shfl_sync(0xffffffffu, r0, l);
+                    const int nl = __shfl_sync(0xffffffffu, nblk, l);
+                    for (int kk = lane; kk < kTileK; kk += 32) {
+                        const int k = kc + kk;
+                        tile[w][l][kk] = k < nl ? (T)v64[r0l * BB + (int64_t)e * nl + k] : T(0);
+                    }
+                }
+                __syncwarp();
+                const int kend = min(kTileK, wdt - kc);
+                for (int kk = 0; kk < kend; ++kk) sval[((b0 + kc + kk) * BB + e) * 32 + lane] = tile[w][lane][kk];
+                __syncwarp();
+            }
     }
 }
+
+static int tile_grid(int64_t ns) { return (int)std::min<int64_t>((ns + kTileWarps - 1) / kTileWarps, 152 * 32); }
 
 void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st)
 {
@@ -76,18 +98,22 @@ void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st)
     if (want64 && !A.s64_valid) {
         A.s64.resize(nv);
         if (A.bs == 3)
-            k_sell_values<3, double><<<g, 256, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p, A.sptr.p, A.s64.p);
+            k_sell_values<3, double><<<tile_grid(A.ns), 32 * kTileWarps, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p,
+                                                                               A.sptr.p, A.s64.p);
         else
-            k_sell_values<1, double><<<g, 256, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p, A.sptr.p, A.s64.p);
+            k_sell_values<1, double><<<tile_grid(A.ns), 32 * kTileWarps, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p,
+                                                                               A.sptr.p, A.s64.p);
         PFG_CUDA(cudaGetLastError());
         A.s64_valid = true;
     }
     if (want32 && !A.s32_valid) {
         A.s32.resize(nv);
         if (A.bs == 3)
-            k_sell_values<3, float><<<g, 256, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p, A.sptr.p, A.s32.p);
+            k_sell_values<3, float><<<tile_grid(A.ns), 32 * kTileWarps, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p,
+                                                                              A.sptr.p, A.s32.p);
         else
-            k_sell_values<1, float><<<g, 256, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p, A.sptr.p, A.s32.p);
+            k_sell_values<1, float><<<tile_grid(A.ns), 32 * kTileWarps, 0, st>>>(A.nb, A.ns, A.rp.p, A.v64.p,
+                                                                              A.sptr.p, A.s32.p);
         PFG_CUDA(cudaGetLastError());
         A.s32_valid = true;
     }
@@ -111,32 +137,61 @@ __global__ void k_sellu_widths(int64_t nb, int64_t ns, const int64_t *__restrict
     }
 }
 
-// columns (and FP32 values) of the upper blocks of each row, in the row's
-// order; padding slots point at the row itself with zero values
-__global__ void k_sellu_fill(int64_t nb, int64_t ns, const int64_t *__restrict__ rp, const int *__restrict__ bcol,
-                             const double *__restrict__ v64, const int64_t *__restrict__ sptr, int *__restrict__ scol,
-                             float *__restrict__ sval)
+// Columns and FP32 values of the upper blocks (column >= row) of each row, in
+// the row's order; padding slots point at the row itself with zero values.
+// One warp per slice, kTileK slots at a time: per row, the ballot prefix of
+// "upper" over its blocks gives each upper block its slot (kept in shared
+// memory), then each entry plane is gathered row by row and written back slot
+// by slot as 32 consecutive lanes.
+__global__ void __launch_bounds__(32 * kTileWarps)
+    k_sellu_fill(int64_t nb, int64_t ns, const int64_t *__restrict__ rp, const int *__restrict__ bcol,
+                 const double *__restrict__ v64, const int64_t *__restrict__ sptr, int *__restrict__ scol,
+                 float *__restrict__ sval)
 {
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ns * 32; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = t >> 5;
-        const int l = (int)(t & 31);
-        const int64_t row = t;
-        const int64_t b0 = sptr[s], w = sptr[s + 1] - b0;
+    __shared__ short kmap[kTileWarps][32][kTileK];
+    __shared__ int ucnt[kTileWarps][32];
+    __shared__ float tile[kTileWarps][32][kTileK + 1];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t s = (int64_t)blockIdx.x * kTileWarps + w; s < ns; s += (int64_t)gridDim.x * kTileWarps) {
+        const int64_t b0 = sptr[s];
+        const int wdt = (int)(sptr[s + 1] - b0);
+        const int64_t row = s * 32 + lane;
         const int64_t r0 = row < nb ? rp[row] : 0;
-        const int64_t nblk = row < nb ? rp[row + 1] - r0 : 0;
-        const int self = row < nb ? (int)row : 0;
-        int64_t slot = 0;
-        for (int64_t k = 0; k < nblk; ++k) {
-            const int c = bcol[r0 + k];
-            if (c < row) continue;
-            scol[(b0 + slot) * 32 + l] = c;
-            for (int e = 0; e < 9; ++e)
-                sval[((b0 + slot) * 9 + e) * 32 + l] = (float)v64[r0 * 9 + (int64_t)e * nblk + k];
-            ++slot;
-        }
-        for (; slot < w; ++slot) {
-            scol[(b0 + slot) * 32 + l] = self;
-            for (int e = 0; e < 9; ++e) sval[((b0 + slot) * 9 + e) * 32 + l] = 0.f;
+        const int nblk = row < nb ? (int)(rp[row + 1] - r0) : 0;
+        for (int kc = 0; kc < wdt; kc += kTileK) {
+            // slots [kc, kc + kTileK) of every row: which of its blocks fill them
+            for (int l = 0; l < 32; ++l) {
+                const int64_t r0l = __shfl_sync(0xffffffffu, r0, l);
+                const int nl = __shfl_sync(0xffffffffu, nblk, l);
+                const int64_t rowl = s * 32 + l;
+                int base = 0;
+                for (int k0 = 0; k0 < nl; k0 += 32) {
+                    const int k = k0 + lane;
+                    const bool up = k < nl && bcol[r0l + k] >= rowl;
+                    const unsigned bal = __ballot_sync(0xffffffffu, up);
+                    const int pos = base + __popc(bal & ((1u << lane) - 1u)) - kc;
+                    if (up && pos >= 0 && pos < kTileK) kmap[w][l][pos] = (short)k;
+                    base += __popc(bal);
+                }
+                if (lane == 0) ucnt[w][l] = min(max(base - kc, 0), kTileK);
+            }
+            __syncwarp();
+            const int kend = min(kTileK, wdt - kc);
+            const int mine = ucnt[w][lane];
+            for (int kk = 0; kk < kend; ++kk)
+                scol[(b0 + kc + kk) * 32 + lane] = kk < mine ? bcol[r0 + kmap[w][lane][kk]] : (row < nb ? (int)row : 0);
+            for (int e = 0; e < 9; ++e) {
+                for (int l = 0; l < 32; ++l) {
+                    const int64_t r0l = __shfl_sync(0xffffffffu, r0, l);
+                    const int nl = __shfl_sync(0xffffffffu, nblk, l);
+                    const int cl = ucnt[w][l];
+                    for (int kk = lane; kk < kTileK; kk += 32)
+                        tile[w][l][kk] = kk < cl ? (float)v64[r0l * 9 + (int64_t)e * nl + kmap[w][l][kk]] : 0.f;
+                }
+                __syncwarp();
+                for (int kk = 0; kk < kend; ++kk) sval[((b0 + kc + kk) * 9 + e) * 32 + lane] = tile[w][lane][kk];
+                __syncwarp();
+            }
         }
     }
 }
@@ -144,46 +199,55 @@ __global__ void k_sellu_fill(int64_t nb, int64_t ns, const int64_t *__restrict__
 // Counts the upper blocks (i, j) whose transpose partner (j, i) is missing or
 // differs by more than 1e-9 relative (plus 1e-12 of the diagonal scale of the
 // two rows: assembly rounding leaves noise in entries that cancel to zero).
+// One warp per row i, a lane per block (i, j): the lane finds (j, i) and row
+// j's diagonal block in one pass over row j's block columns.
 __global__ void k_sym_check(int64_t nb, const int64_t *__restrict__ rp, const int *__restrict__ bcol,
                             const double *__restrict__ v64, unsigned long long *__restrict__ bad)
 {
-    auto entry = [&](int64_t row, int64_t k, int e) {
-        const int64_t r0 = rp[row];
-        return v64[r0 * 9 + (int64_t)e * (rp[row + 1] - r0) + k];
-    };
-    auto diag_scale = [&](int64_t row) {
-        double m = 0.0;
-        for (int64_t k = rp[row]; k < rp[row + 1]; ++k)
-            if (bcol[k] == row)
-                for (int e = 0; e < 9; e += 4) m = fmax(m, fabs(entry(row, k - rp[row], e)));
-        return m;
-    };
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
-        const double di = diag_scale(i);
-        for (int64_t k = rp[i]; k < rp[i + 1]; ++k) {
-            const int64_t j = bcol[k];
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t i = w0; i < nb; i += nw) {
+        const int64_t ri = rp[i];
+        const int ni = (int)(rp[i + 1] - ri);
+        // |diagonal entries| of row i's diagonal block
+        double di = 0.0;
+        for (int k = lane; k < ni; k += 32)
+            if (bcol[ri + k] == i)
+                for (int e = 0; e < 9; e += 4) di = fmax(di, fabs(v64[ri * 9 + (int64_t)e * ni + k]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) di = fmax(di, __shfl_xor_sync(0xffffffffu, di, o));
+        unsigned long long nbad = 0;
+        for (int k = lane; k < ni; k += 32) {
+            const int64_t j = bcol[ri + k];
             if (j <= i) continue;
-            int64_t kk = -1;
-            for (int64_t q = rp[j]; q < rp[j + 1]; ++q)
-                if (bcol[q] == i) {
-                    kk = q - rp[j];
-                    break;
-                }
+            const int64_t rj = rp[j];
+            const int nj = (int)(rp[j + 1] - rj);
+            int kk = -1;
+            double dj = 0.0;
+            for (int q = 0; q < nj; ++q) {
+                const int64_t c = bcol[rj + q];
+                if (c == i && kk < 0) kk = q;
+                if (c == j)
+                    for (int e = 0; e < 9; e += 4) dj = fmax(dj, fabs(v64[rj * 9 + (int64_t)e * nj + q]));
+            }
             if (kk < 0) {
-                atomicAdd(bad, 1ull);
+                ++nbad;
                 continue;
             }
-            const double scale = 1e-12 * fmax(di, diag_scale(j));
+            const double scale = 1e-12 * fmax(di, dj);
+            bool ok = true;
+#pragma unroll
             for (int r = 0; r < 3; ++r)
+#pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const double a = entry(i, k - rp[i], 3 * r + c), b = entry(j, kk, 3 * c + r);
-                    if (!(fabs(a - b) <= 1e-9 * fmax(fabs(a), fabs(b)) + scale)) {
-                        atomicAdd(bad, 1ull);
-                        r = 3;
-                        break;
-                    }
+                    const double a = v64[ri * 9 + (int64_t)(3 * r + c) * ni + k];
+                    const double b = v64[rj * 9 + (int64_t)(3 * c + r) * nj + kk];
+                    ok = ok && fabs(a - b) <= 1e-9 * fmax(fabs(a), fabs(b)) + scale;
                 }
+            nbad += !ok;
         }
+        if (nbad) atomicAdd(bad, nbad);
     }
 }
 
@@ -218,7 +282,8 @@ void build_sell_upper(DevMatrix &A, cudaStream_t st)
         A.s32_u.resize((size_t)std::max<int64_t>(slots * 32 * 9, 1));
         A.sell_u_pattern = true;
     }
-    k_sellu_fill<<<g, 256, 0, st>>>(A.nb, A.ns_u, A.rp.p, A.col.p, A.v64.p, A.sptr_u.p, A.scol_u.p, A.s32_u.p);
+    k_sellu_fill<<<tile_grid(A.ns_u), 32 * kTileWarps, 0, st>>>(A.nb, A.ns_u, A.rp.p, A.col.p, A.v64.p, A.sptr_u.p,
+                                                               A.scol_u.p, A.s32_u.p);
     PFG_CUDA(cudaGetLastError());
     A.s32_u_valid = true;
 }
