@@ -460,9 +460,10 @@ def newmark_lines(n=60, steps=40, dt=1e-3):
         sa.LinearReyleighNewmark(TOL=1e-10, precision=prec, storage=storage)  # set-up and first step
         t = time.perf_counter()
         its = 0
-        for _ in range(steps):
-            sa.LinearReyleighNewmark(TOL=1e-10, precision=prec, storage=storage)
-            its += sa.last_info["iterations"]
+        with _nvtx(f"newmark_{prec}"):  # profiler filter (ncu --nvtx-include)
+            for _ in range(steps):
+                sa.LinearReyleighNewmark(TOL=1e-10, precision=prec, storage=storage)
+                its += sa.last_info["iterations"]
         wall = (time.perf_counter() - t) / steps
         res[prec] = sa.U.copy()
         out[prec] = {"ms_per_step": round(wall * 1e3, 3), "steps_per_s": round(1.0 / wall, 2),

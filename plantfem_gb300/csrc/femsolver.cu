@@ -505,7 +505,7 @@ int pfg_dev_spmv(pfg_solver *h, const double *d_x, double *d_y, void *stream)
         flush_pending(h);
         cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
         if (st != h->st) PFG_CUDA(cudaStreamSynchronize(h->st));
-        Krylov::spmv64(h->K, d_x, d_y, st);
+        Krylov::spmv64_sliced(h->K, d_x, d_y, st);
         if (!stream) PFG_CUDA(cudaStreamSynchronize(st));  // own stream: done on return
     });
 }
@@ -874,7 +874,8 @@ int pfg_ilu_apply(pfg_solver *h, const double *v, double *out)
         const int64_t n = h->ndof();
         DevBuf<double> dv((size_t)n), dout((size_t)n);
         PFG_CUDA(cudaMemcpyAsync(dv.p, v, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
-        const Ilu0 &f = h->kry.ilu_factor(h->K, true, h->st);
+        const Ilu0 *held = h->kry.ilu_held();
+        const Ilu0 &f = held ? *held : h->kry.ilu_factor(h->K, true, h->st);
         f.apply(dv.p, dout.p, nullptr, h->st);
         PFG_CUDA(cudaMemcpyAsync(out, dout.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
         PFG_CUDA(cudaStreamSynchronize(h->st));
@@ -1131,8 +1132,8 @@ int pfg_newmark_step(pfg_solver *h, const pfg_solve_opts *opts, int64_t n, const
         k_newmark_weights<<<gv, 256, 0, h->st>>>(n, a_ext ? nm.tmp.p : nullptr, nm.u.p, nm.v.p, nm.a.p, mu, mv, ma,
                                                  ku, kv, ka, nm.wM.p, nm.wK.p);
         PFG_CUDA(cudaGetLastError());
-        Krylov::spmv64(*Mp, nm.wM.p, nm.rhs.p, h->st);
-        Krylov::spmv64(*Kp, nm.wK.p, nm.tmp.p, h->st);
+        Krylov::spmv64_sliced(*Mp, nm.wM.p, nm.rhs.p, h->st);
+        Krylov::spmv64_sliced(*Kp, nm.wK.p, nm.tmp.p, h->st);
         k_newmark_rhs<<<gv, 256, 0, h->st>>>(n, nm.rhs.p, nm.tmp.p, nm.base.p, h->have_fix ? h->fixed_d.p : nullptr);
         PFG_CUDA(cudaGetLastError());
         // A_eff u' = rhs from the previous displacement

@@ -1118,6 +1118,8 @@ const Ilu0 &Krylov::ilu_factor(const DevMatrix &A, bool sorted, cudaStream_t st)
     return *ilu_;
 }
 
+const Ilu0 *Krylov::ilu_held() const { return ilu_ && ilu_->ready() ? ilu_.get() : nullptr; }
+
 void Krylov::ilu_reset()
 {
     if (ilu_) ilu_->reset();
@@ -1137,6 +1139,19 @@ void Krylov::spmv64(const DevMatrix &A, const double *x, double *y, cudaStream_t
         launch_spmv<3, double>(A, A.view<double>(), x, y, st);
     else
         launch_spmv<1, double>(A, A.view<double>(), x, y, st);
+}
+
+void Krylov::spmv64_sliced(DevMatrix &A, const double *x, double *y, cudaStream_t st)
+{
+    if (A.nb == 0) return;
+    build_sell(A, true, false, st);
+    if (A.bs == 3)
+        k_spmv_sell<3, double><<<resident_grid(k_spmv_sell<3, double>, A.ns), kThreads, 0, st>>>(A.sell<double>(), x,
+                                                                                                 y);
+    else
+        k_spmv_sell<1, double><<<resident_grid(k_spmv_sell<1, double>, A.ns), kThreads, 0, st>>>(A.sell<double>(), x,
+                                                                                                 y);
+    PFG_CUDA(cudaGetLastError());
 }
 
 void Krylov::spmv32(const DevMatrix &A, const float *x, float *y, cudaStream_t st)

@@ -144,6 +144,9 @@ class Krylov {
     SolveResult solve(DevMatrix &A, const double *b, double *x, const KConfig &cfg, cudaStream_t st);
     // y = A x in FP64 / FP32 (plain SpMV, used by the C ABI and the tests).
     static void spmv64(const DevMatrix &A, const double *x, double *y, cudaStream_t st);
+    // y = A x in FP64 from the sliced copy (built on first use and kept while
+    // the values stay): the form for a matrix that is applied many times.
+    static void spmv64_sliced(DevMatrix &A, const double *x, double *y, cudaStream_t st);
     static void spmv32(const DevMatrix &A, const float *x, float *y, cudaStream_t st);
     static void make_v32(DevMatrix &A, cudaStream_t st);
     // Grid size used for the row loops (a multiple of the SM count).
@@ -156,6 +159,8 @@ class Krylov {
     // The ILU(0) factor kept for PFG_PC_ILU0* solves (ilu.cuh); factored from
     // A (if not held for A's pattern and this column order) by ilu_factor.
     const Ilu0 &ilu_factor(const DevMatrix &A, bool sorted, cudaStream_t st);
+    // The factor held now (null if none).
+    const Ilu0 *ilu_held() const;
     void ilu_reset();
 
   private:

@@ -91,6 +91,7 @@ void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st)
         A.sell_pattern = true;
         A.s64_valid = A.s32_valid = false;
     }
+    if (!(want64 && !A.s64_valid) && !(want32 && !A.s32_valid)) return;  // up to date: no host round trip
     int64_t slots = 0;
     PFG_CUDA(cudaMemcpyAsync(&slots, A.sptr.p + A.ns, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     PFG_CUDA(cudaStreamSynchronize(st));

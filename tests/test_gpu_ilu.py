@@ -186,6 +186,25 @@ def test_ilu_stored_order_on_fem_rows(cuda):
     assert failed
 
 
+def test_ilu_apply_uses_the_held_factor(cuda):
+    """ILU_matvec applies the factor the solver keeps, whichever order it was
+    taken in (it does not refactor)."""
+    rp, ci, v = _scalar_matrix(40, 5)
+    rng = np.random.default_rng(2)
+    for i in range(rp.shape[0] - 1):
+        a, b = rp[i] - 1, rp[i + 1] - 1
+        q = a + rng.permutation(b - a)
+        ci[a:b], v[a:b] = ci[q].copy(), v[q].copy()
+    s = FEMSolver()
+    s.setCRS(CRS=(rp, ci, v))
+    lu = s.ILU(sorted=False)
+    w = rng.standard_normal(rp.shape[0] - 1)
+    out = s.ILU_matvec(w)
+    ref = O.ilu_apply(rp, ci, lu, w)
+    assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.array_equal(s.ILU(sorted=False), lu)
+
+
 def test_ilu_refuses_cg_and_mixed(cuda):
     s, p = _fem(3)
     s.eliminate()
