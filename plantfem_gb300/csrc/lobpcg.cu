@@ -35,8 +35,9 @@ static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
         if (vv == 0.0) continue;
         const double beta = 2.0 / vv;
         // A <- H A H with H = I - beta v v^T:  p = beta A v, K = beta/2 v^T p, q = p - K v,
-        // A <- A - v q^T - q v^T
-        for (int i = 0; i < n; ++i) {
+        // A <- A - v q^T - q v^T.  Columns < j are reduced already (zero below
+        // their subdiagonal), so p, q and the update live in rows/columns >= j.
+        for (int i = j; i < n; ++i) {
             double s = 0.0;
             for (int l = j + 1; l < n; ++l) s += a(i, l) * v[l];
             p[i] = beta * s;
@@ -44,9 +45,9 @@ static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
         double K = 0.0;
         for (int i = j + 1; i < n; ++i) K += v[i] * p[i];
         K *= 0.5 * beta;
-        for (int i = 0; i < n; ++i) q[i] = p[i] - K * v[i];
-        for (int c = 0; c < n; ++c)
-            for (int r = 0; r < n; ++r) a(r, c) -= v[r] * q[c] + q[r] * v[c];
+        for (int i = j; i < n; ++i) q[i] = p[i] - K * v[i];
+        for (int c = j; c < n; ++c)
+            for (int r = j; r < n; ++r) a(r, c) -= v[r] * q[c] + q[r] * v[c];
         // Q <- Q H
         for (int r = 0; r < n; ++r) {
             double s = 0.0;
@@ -68,15 +69,17 @@ static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
                 if (std::fabs(e[m]) <= eps * dd) break;
             }
             if (m == l) break;
+            // sqrt(x*x + y*y) in place of hypot: the matrices are scaled to
+            // unit diagonal (B) or come from it (A'), far from overflow
             double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-            double r = std::hypot(g, 1.0);
+            double r = std::sqrt(g * g + 1.0);
             g = d[m] - d[l] + e[l] / (g + (g >= 0 ? r : -r));
             double s = 1.0, c = 1.0, pp = 0.0;
             int i = m - 1;
             bool underflow = false;
             for (; i >= l; --i) {
                 const double f = s * e[i], b = c * e[i];
-                r = std::hypot(f, g);
+                r = std::sqrt(f * f + g * g);
                 e[i + 1] = r;
                 if (r == 0.0) {
                     d[i + 1] -= pp;
