@@ -331,7 +331,8 @@ def modal_lines(n=60, nev=20, block=24, tol=1e-8):
     lams = {}
     for prec in ("fp64", "mixed"):
         try:
-            lam, _ = s.eig(nev, block_size=block, precision=prec, eigen_vectors=False)
+            with _nvtx(f"modal_{prec}"):  # profiler filter (ncu --nvtx-include)
+                lam, _ = s.eig(nev, block_size=block, precision=prec, eigen_vectors=False)
             i = s.last_info
             lams[prec] = lam
             out[prec] = {"ms": round(i["solve_ms"], 1), "iterations": i["iterations"],
