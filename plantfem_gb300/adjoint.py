@@ -1,6 +1,7 @@
 """Differentiable solve: u(E) with dL/dE by one adjoint solve.
 
-The reference has no adjoint; this is the benchmark spec's differentiation form.
+The reference has no adjoint; this is the path's differentiation form (dL/dE of
+the linear-elastic solve for per-element Young's moduli).
 For the eliminated system K(E) u = f (Dirichlet rows/columns removed, as
 FEMSolver_%solve does, FEMSolverClass.f90:1707-1756) and a loss L(u),
 

@@ -5,7 +5,7 @@ Tolerances: index arrays are compared bit for bit; the elimination is bit for
 bit given the same assembled values; assembled values within 1e-12 of the
 largest entry (different summation order of element contributions); SpMV
 within 1e-13 relative (warp-tree vs serial row sums); solutions within 1e-8
-relative to the FP64 oracle solved to 1e-12 (the benchmark spec's bar).
+relative to the FP64 oracle solved to 1e-12 (the accuracy bar of the path).
 """
 import os
 
