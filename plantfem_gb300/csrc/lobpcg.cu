@@ -48,12 +48,17 @@ static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
         for (int i = j; i < n; ++i) q[i] = p[i] - K * v[i];
         for (int c = j; c < n; ++c)
             for (int r = j; r < n; ++r) a(r, c) -= v[r] * q[c] + q[r] * v[c];
-        // Q <- Q H
-        for (int r = 0; r < n; ++r) {
-            double s = 0.0;
-            for (int l = j + 1; l < n; ++l) s += Q[(size_t)l * n + r] * v[l];
-            s *= beta;
-            for (int l = j + 1; l < n; ++l) Q[(size_t)l * n + r] -= s * v[l];
+        // Q <- Q H = Q - beta (Q v) v^T, column by column (contiguous)
+        for (int r = 0; r < n; ++r) p[r] = 0.0;
+        for (int l = j + 1; l < n; ++l) {
+            const double vl = v[l];
+            const double *ql = &Q[(size_t)l * n];
+            for (int r = 0; r < n; ++r) p[r] += ql[r] * vl;
+        }
+        for (int l = j + 1; l < n; ++l) {
+            const double bv = beta * v[l];
+            double *ql = &Q[(size_t)l * n];
+            for (int r = 0; r < n; ++r) ql[r] -= p[r] * bv;
         }
     }
     for (int i = 0; i < n; ++i) d[i] = a(i, i);
@@ -118,6 +123,28 @@ static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
     }
 }
 
+// B = L L^T (lower L, column-major, in place of B's lower triangle) when every
+// pivot exceeds rank_tol times the largest diagonal entry; false otherwise.
+static bool cholesky_well_posed(int m, std::vector<double> &B, double rank_tol)
+{
+    double dmax = 0.0;
+    for (int i = 0; i < m; ++i) dmax = std::max(dmax, B[(size_t)i * m + i]);
+    if (!(dmax > 0.0)) return false;
+    for (int j = 0; j < m; ++j) {
+        double d = B[(size_t)j * m + j];
+        for (int l = 0; l < j; ++l) d -= B[(size_t)l * m + j] * B[(size_t)l * m + j];
+        if (!(d > rank_tol * dmax)) return false;
+        const double ljj = std::sqrt(d);
+        B[(size_t)j * m + j] = ljj;
+        for (int i = j + 1; i < m; ++i) {
+            double v = B[(size_t)j * m + i];
+            for (int l = 0; l < j; ++l) v -= B[(size_t)l * m + i] * B[(size_t)l * m + j];
+            B[(size_t)j * m + i] = v / ljj;
+        }
+    }
+    return true;
+}
+
 int small_generalized_eig(int m, const double *Ain, const double *Bin, int k, double rank_tol, double *lam, double *C)
 {
     // scale to unit diagonal, then keep B's numerically nonzero directions
@@ -130,6 +157,52 @@ int small_generalized_eig(int m, const double *Ain, const double *Bin, int k, do
     for (int j = 0; j < m; ++j)
         for (int i = 0; i < m; ++i)
             B[(size_t)j * m + i] = 0.5 * (Bin[(size_t)j * m + i] + Bin[(size_t)i * m + j]) * s[i] * s[j];
+    {
+        // Well-posed B (no pivot at or below rank_tol of the largest: the
+        // usual case): A' = L^-1 (S A S) L^-T and C = S L^-T Y, a Cholesky
+        // and two triangular solves instead of B's eigendecomposition.
+        // Otherwise B's eigendecomposition below drops its null directions.
+        std::vector<double> L = B;
+        if (cholesky_well_posed(m, L, rank_tol)) {
+            auto l = [&](int i, int j) { return L[(size_t)j * m + i]; };
+            // W = L^-1 (S A S): forward substitution on each column
+            std::vector<double> W((size_t)m * m);
+            for (int c = 0; c < m; ++c)
+                for (int i = 0; i < m; ++i) {
+                    double v = 0.5 * (Ain[(size_t)c * m + i] + Ain[(size_t)i * m + c]) * s[i] * s[c];
+                    for (int q = 0; q < i; ++q) v -= l(i, q) * W[(size_t)c * m + q];
+                    W[(size_t)c * m + i] = v / l(i, i);
+                }
+            // A' = W L^-T = (L^-1 W^T)^T: forward substitution on W's rows
+            std::vector<double> Ap((size_t)m * m);
+            for (int r = 0; r < m; ++r)
+                for (int i = 0; i < m; ++i) {
+                    double v = W[(size_t)i * m + r];
+                    for (int q = 0; q < i; ++q) v -= l(i, q) * Ap[(size_t)q * m + r];
+                    Ap[(size_t)i * m + r] = v / l(i, i);
+                }
+            for (int c = 0; c < m; ++c)
+                for (int i = 0; i < c; ++i) {
+                    const double v = 0.5 * (Ap[(size_t)c * m + i] + Ap[(size_t)i * m + c]);
+                    Ap[(size_t)c * m + i] = Ap[(size_t)i * m + c] = v;
+                }
+            std::vector<double> mu;
+            sym_eig(m, Ap, mu);
+            const int kk = std::min(k, m);
+            for (int j = 0; j < kk; ++j) {
+                lam[j] = mu[j];
+                // y = column j of the eigenvectors; C_j = S L^-T y (back substitution)
+                double *cj = C + (size_t)j * m;
+                for (int i = m - 1; i >= 0; --i) {
+                    double v = Ap[(size_t)j * m + i];
+                    for (int q = i + 1; q < m; ++q) v -= l(q, i) * cj[q];
+                    cj[i] = v / l(i, i);
+                }
+                for (int i = 0; i < m; ++i) cj[i] *= s[i];
+            }
+            return kk;
+        }
+    }
     sym_eig(m, B, w);
     const double wmax = w[m - 1];
     if (!(wmax > 0)) return 0;
