@@ -1513,7 +1513,8 @@ SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfi
     launches_ = 0;
     // the Krylov kernels read the sliced copy: FP64 always (residuals), FP32
     // for the mixed inner iterations
-    build_sell(A, true, cfg.precision == PFG_PREC_MIXED, st);
+    // the symmetric-storage inner iterations read only the upper-half FP32 copy
+    build_sell(A, true, cfg.precision == PFG_PREC_MIXED && cfg.storage != PFG_STORAGE_SYMMETRIC, st);
     cudaEvent_t e0, e1;
     PFG_CUDA(cudaEventCreate(&e0));
     PFG_CUDA(cudaEventCreate(&e1));
@@ -1726,10 +1727,8 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
 {
     SolveResult res;
     const bool cg = cfg.algorithm == PFG_ALG_CG;
-    if (!A.v32_valid) {
-        make_v32(A, st);
-        ++launches_;
-    }
+    // the FP32 sliced copies come from the FP64 values (build_sell,
+    // build_sell_upper): no FP32 block-row copy is needed here
     build_precond(A, cfg.precond, true, st);
     const int64_t n = A.ndof();
     const int g = row_grid(A.nb);
