@@ -217,6 +217,13 @@ int pfg_ilu_factor(pfg_solver *h, int32_t sorted, double *lu_out);
  * vectors of pfg ndof values. */
 int pfg_ilu_apply(pfg_solver *h, const double *v, double *out);
 
+/* CRS_%ILU(0, RHS) (ILUCRS's RHS branch, SparseClass.f90:1647-1679): x = the
+ * solve with the held factor (taken in ascending order first if none is held):
+ * forward substitution with L, division by U's diagonal where nonzero, then
+ * backward substitution with U.  The reference factors its matrix in place
+ * first; here the handle's matrix is left as it is.  Host vectors. */
+int pfg_ilu_solve(pfg_solver *h, const double *rhs, double *x);
+
 /* ------------------------------------------------------------- eigenproblem */
 /* FEMSolver_%keepThisMatrixAs(As) (FEMSolverClass.f90:1544-1604): copy the
  * working matrix into a named slot ("A" = stiffness, "B" = mass for eig); at

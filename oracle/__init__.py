@@ -74,6 +74,7 @@ def lib():
     L.orc_reduce_crs.restype = C.c_int64
     L.orc_ilu0.argtypes = [C.c_int64, _i64, _i32, _d, C.c_int]
     L.orc_ilu_apply.argtypes = [C.c_int64, _i64, _i32, _d, _d, _d]
+    L.orc_ilu_solve.argtypes = [C.c_int64, _i64, _i32, _d, _d]
     L.orc_bicgstab_ilu.argtypes = [C.c_int64, _i64, _i32, _d, _d, _d, _d, C.c_int, C.c_double, C.c_double,
                                    C.POINTER(C.c_int)]
     L.orc_num_threads.restype = C.c_int
@@ -258,6 +259,13 @@ def ilu_apply(row_ptr, col_idx, lu, v):
     out = np.zeros(row_ptr.shape[0] - 1)
     lib().orc_ilu_apply(out.shape[0], row_ptr, col_idx, lu, np.ascontiguousarray(v, dtype=np.float64), out)
     return out
+
+
+def ilu_solve(row_ptr, col_idx, lu, rhs):
+    """ILUCRS(0, RHS) (SparseClass.f90:1647-1679) with the factor lu -> the solution."""
+    x = np.array(rhs, dtype=np.float64)
+    lib().orc_ilu_solve(x.shape[0], row_ptr, col_idx, lu, x)
+    return x
 
 
 def bicgstab_ilu(row_ptr, col_idx, val, b, lu=None, sorted=False, x0=None, itrmax=100000, er0=1e-10,

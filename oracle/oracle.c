@@ -891,3 +891,25 @@ done:
     free(r); free(r0); free(p); free(y); free(e); free(v); free(pd); free(ps);
     return rc;
 }
+
+/* ILUCRS(0, RHS) (SparseClass.f90:1647-1679), the solve with an ILU(0) factor   */
+/* lu (orc_ilu0), in place on rhs: forward substitution with the unit lower    */
+/* factor; rhs(i) /= U(i,i) where U(i,i) != 0; then for i = n..1,              */
+/* rhs(i) -= U(i,j)/U(i,i) rhs(j) over the entries j > i (this loop divides by */
+/* a zero U(i,i), as the reference does).                                      */
+void orc_ilu_solve(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, const double *lu, double *rhs)
+{
+    double *d = calloc((size_t)n, sizeof(double));
+    for (int64_t i = 0; i < n; ++i)
+        for (int64_t q = row_ptr[i] - 1; q < row_ptr[i + 1] - 1; ++q)
+            if (col_idx[q] - 1 == i) { d[i] = lu[q]; break; }
+    for (int64_t i = 1; i < n; ++i)
+        for (int64_t q = row_ptr[i] - 1; q < row_ptr[i + 1] - 1; ++q)
+            if (col_idx[q] - 1 < i) rhs[i] = rhs[i] - lu[q] * rhs[col_idx[q] - 1];
+    for (int64_t i = n - 1; i >= 0; --i)
+        if (d[i] != 0.0) rhs[i] = rhs[i] / d[i];
+    for (int64_t i = n - 1; i >= 0; --i)
+        for (int64_t q = row_ptr[i] - 1; q < row_ptr[i + 1] - 1; ++q)
+            if (col_idx[q] - 1 > i) rhs[i] = rhs[i] - lu[q] / d[i] * rhs[col_idx[q] - 1];
+    free(d);
+}

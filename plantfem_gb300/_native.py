@@ -129,6 +129,7 @@ SIGNATURES = {
     "pfg_ilu_reset": (C.c_int, [_P]),
     "pfg_ilu_factor": (C.c_int, [_P, C.c_int32, _P]),
     "pfg_ilu_apply": (C.c_int, [_P, _P, _P]),
+    "pfg_ilu_solve": (C.c_int, [_P, _P, _P]),
     "pfg_element_stress": (C.c_int, [_P, _P, _i64, _P, _P, _i32, _P]),
     "pfg_dev_assemble_stiffness": (C.c_int, [_P, _i64, _P, _P, _P]),
     "pfg_dev_set_rhs": (C.c_int, [_P, _i64, _P, _P]),

@@ -882,6 +882,24 @@ int pfg_ilu_apply(pfg_solver *h, const double *v, double *out)
     });
 }
 
+int pfg_ilu_solve(pfg_solver *h, const double *rhs, double *x)
+{
+    return guard([&] {
+        need(h && rhs && x, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        need(h->have_crs, PFG_E_STATE, "ILU(0) before setCRS");
+        flush_pending(h);
+        const int64_t n = h->ndof();
+        DevBuf<double> dr((size_t)n), dx((size_t)n);
+        PFG_CUDA(cudaMemcpyAsync(dr.p, rhs, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        const Ilu0 *held = h->kry.ilu_held();
+        const Ilu0 &f = held ? *held : h->kry.ilu_factor(h->K, true, h->st);
+        f.solve(dr.p, dx.p, h->st);
+        PFG_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+        PFG_CUDA(cudaStreamSynchronize(h->st));
+    });
+}
+
 int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop, const double *E, const double *v,
                        int32_t option, double *out)
 {

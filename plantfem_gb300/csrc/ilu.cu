@@ -155,7 +155,10 @@ __global__ void __launch_bounds__(32 * kIluWarps)
 template <int BS>
 constexpr int diag_stride() { return BS == 3 ? 8 : 1; }  // [l10 l20 l21 r0 r1 r2 - -] or [r0]
 
-template <int BS>
+// UPPER: the same layout for the backward solve, with the blocks J > I, the
+// strictly upper part of the diagonal block ([u01 u02 u12 q0 q1 q2 - -] or
+// [q0]) and q = 1 / U(i,i) as the reference divides (a zero U(i,i) gives inf).
+template <int BS, bool UPPER>
 __global__ void __launch_bounds__(32 * kIluWarps)
     k_ilu_sweep_layout(const int64_t *__restrict__ rp, const int *__restrict__ col, const double *__restrict__ lu,
                        const double *__restrict__ udiag, const int *__restrict__ order,
@@ -175,23 +178,27 @@ __global__ void __launch_bounds__(32 * kIluWarps)
     int carry = 0;
     for (int b0 = 0; b0 < nbI; b0 += 32) {
         const int b = b0 + lane;
-        const int J = b < nbI ? col[base + b] : INT_MAX;
-        const unsigned low = __ballot_sync(0xffffffffu, J < I);
-        if (J < I) {
-            const int r = carry + __popc(low & ((1u << lane) - 1u));
+        const int J = b < nbI ? col[base + b] : (UPPER ? -1 : INT_MAX);
+        const bool take = UPPER ? J > I : J < I;
+        const unsigned sel = __ballot_sync(0xffffffffu, take);
+        if (take) {
+            const int r = carry + __popc(sel & ((1u << lane) - 1u));
             sw_col[off + r] = J;
 #pragma unroll
             for (int rc = 0; rc < BB; ++rc) sw_val[BB * off + (int64_t)rc * m + r] = lu[BB * base + (int64_t)rc * nbI + b];
         } else if (J == I && BS == 3) {
-            sw_diag[SD * p + 0] = lu[BB * base + (int64_t)(1 * BS + 0) * nbI + b];
-            sw_diag[SD * p + 1] = lu[BB * base + (int64_t)(2 * BS + 0) * nbI + b];
-            sw_diag[SD * p + 2] = lu[BB * base + (int64_t)(2 * BS + 1) * nbI + b];
+            const int e0 = UPPER ? 0 * BS + 1 : 1 * BS + 0;
+            const int e1 = UPPER ? 0 * BS + 2 : 2 * BS + 0;
+            const int e2 = UPPER ? 1 * BS + 2 : 2 * BS + 1;
+            sw_diag[SD * p + 0] = lu[BB * base + (int64_t)e0 * nbI + b];
+            sw_diag[SD * p + 1] = lu[BB * base + (int64_t)e1 * nbI + b];
+            sw_diag[SD * p + 2] = lu[BB * base + (int64_t)e2 * nbI + b];
         }
-        carry += __popc(low);
+        carry += __popc(sel);
     }
     if (lane < BS) {
         const double d = udiag[(int64_t)BS * I + lane];
-        sw_diag[SD * p + (BS == 3 ? 3 : 0) + lane] = d == 0.0 ? 1.0 : 1.0 / d;
+        sw_diag[SD * p + (BS == 3 ? 3 : 0) + lane] = UPPER ? 1.0 / d : (d == 0.0 ? 1.0 : 1.0 / d);
     }
 }
 
@@ -315,6 +322,98 @@ __global__ void __launch_bounds__(32 * kIluWarps)
     }
 }
 
+// The backward half of ILUCRS(0, RHS) (SparseClass.f90:1663-1677) for the block
+// rows of one level of the upper dependency order, in place on x (which holds
+// y_i / U(i,i) from the forward sweep): x_i -= (sum_{j>i} U(i,j) x_j) / U(i,i).
+// Same lane layout and launch scheme as k_ilu_lower; x_j (j > i) is final
+// from earlier levels, read through L2 after the wait.
+template <int BS>
+__global__ void __launch_bounds__(32 * kIluWarps)
+    k_ilu_upper(const int2 *__restrict__ sw_row, const int64_t *__restrict__ sw_off, const int *__restrict__ sw_col,
+                const double *__restrict__ sw_val, const double *__restrict__ sw_diag, int64_t start, int count,
+                double *x)
+{
+    constexpr int BB = BS * BS, SD = diag_stride<BS>();
+    const int sub = threadIdx.x % kSweepLanes;
+    const int idx = blockIdx.x * kSweepRows + threadIdx.x / kSweepLanes;
+    const bool active = idx < count;
+    int I = 0, m = 0;
+    int64_t off = 0;
+    int J[kSweepSlots];
+    double gv[kSweepSlots][BB];
+    double dd[SD], yI[BS];
+#pragma unroll
+    for (int q = 0; q < kSweepSlots; ++q) J[q] = -1;
+    if (active) {
+        const int64_t p = start + idx;
+        const int2 rm = sw_row[p];
+        off = sw_off[p];
+        I = rm.x;
+        m = rm.y;
+#pragma unroll
+        for (int q = 0; q < kSweepSlots; ++q) {
+            const int b = sub + kSweepLanes * q;
+            if (b < m) {
+                J[q] = sw_col[off + b];
+#pragma unroll
+                for (int rc = 0; rc < BB; ++rc) gv[q][rc] = sw_val[BB * off + (int64_t)rc * m + b];
+            }
+        }
+        if (sub == 0) {
+#pragma unroll
+            for (int k = 0; k < SD; ++k) dd[k] = sw_diag[SD * p + k];
+#pragma unroll
+            for (int d = 0; d < BS; ++d) yI[d] = __ldcg(x + (int64_t)BS * I + d);  // from the forward sweep
+        }
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;");
+    double acc[BS];
+#pragma unroll
+    for (int d = 0; d < BS; ++d) acc[d] = 0.0;
+#pragma unroll
+    for (int q = 0; q < kSweepSlots; ++q) {
+        if (J[q] >= 0) {
+            double xj[BS];
+#pragma unroll
+            for (int e = 0; e < BS; ++e) xj[e] = __ldcg(x + (int64_t)BS * J[q] + e);
+#pragma unroll
+            for (int d = 0; d < BS; ++d)
+#pragma unroll
+                for (int e = 0; e < BS; ++e) acc[d] = fma(gv[q][d * BS + e], xj[e], acc[d]);
+        }
+    }
+    for (int b = sub + kSweepLanes * kSweepSlots; b < m; b += kSweepLanes) {
+        const int Jb = sw_col[off + b];
+        double xj[BS];
+#pragma unroll
+        for (int e = 0; e < BS; ++e) xj[e] = __ldcg(x + (int64_t)BS * Jb + e);
+#pragma unroll
+        for (int d = 0; d < BS; ++d)
+#pragma unroll
+            for (int e = 0; e < BS; ++e)
+                acc[d] = fma(sw_val[BB * off + (int64_t)(d * BS + e) * m + b], xj[e], acc[d]);
+    }
+#pragma unroll
+    for (int o = kSweepLanes / 2; o > 0; o >>= 1) {
+#pragma unroll
+        for (int d = 0; d < BS; ++d) acc[d] += __shfl_xor_sync(0xffffffffu, acc[d], o);
+    }
+    if (active && sub == 0) {
+        if constexpr (BS == 3) {
+            const double x2 = yI[2] - acc[2] * dd[5];
+            const double x1 = yI[1] - (acc[1] + dd[2] * x2) * dd[4];
+            const double x0 = yI[0] - (acc[0] + dd[0] * x1 + dd[1] * x2) * dd[3];
+            double *xr = x + (int64_t)3 * I;
+            xr[0] = x0;
+            xr[1] = x1;
+            xr[2] = x2;
+        } else {
+            x[I] = yI[0] - acc[0] * dd[0];
+        }
+    }
+}
+
 // Levels of at most this many block rows launch early (see k_ilu_lower).
 constexpr int kIluEarlyRows = 1024;
 
@@ -337,6 +436,24 @@ void launch_lower(int grid, bool early, const int2 *sw_row, const int64_t *sw_of
     cfg.numAttrs = early ? 1 : 0;
     PFG_CUDA(cudaLaunchKernelEx(&cfg, k_ilu_lower<BS>, sw_row, sw_off, sw_col, sw_val, sw_diag, start, count, v, t,
                                 out, S));
+}
+
+// One level of the backward sweep, launched like launch_lower.
+template <int BS>
+void launch_upper(int grid, bool early, const int2 *sw_row, const int64_t *sw_off, const int *sw_col,
+                  const double *sw_val, const double *sw_diag, int64_t start, int count, double *x, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(32 * kIluWarps);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = early ? 1 : 0;
+    PFG_CUDA(cudaLaunchKernelEx(&cfg, k_ilu_upper<BS>, sw_row, sw_off, sw_col, sw_val, sw_diag, start, count, x));
 }
 
 int ilu_grid(int64_t count) { return (int)((count + kIluWarps - 1) / kIluWarps); }
@@ -411,14 +528,60 @@ void Ilu0::factor(const DevMatrix &A, bool sorted, cudaStream_t st)
     // a row without a stored diagonal block keeps zero lower entries there
     PFG_CUDA(cudaMemsetAsync(sw_diag_.p, 0, sw_diag_.bytes(), st));
     if (A.bs == 3)
-        k_ilu_sweep_layout<3><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(A.rp.p, A.col.p, lu_.p, udiag_.p, order_.p,
+        k_ilu_sweep_layout<3, false><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(A.rp.p, A.col.p, lu_.p, udiag_.p, order_.p,
                                                                         sw_off_.p, A.nb, sw_row_.p, sw_col_.p,
                                                                         sw_val_.p, sw_diag_.p);
     else
-        k_ilu_sweep_layout<1><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(A.rp.p, A.col.p, lu_.p, udiag_.p, order_.p,
+        k_ilu_sweep_layout<1, false><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(A.rp.p, A.col.p, lu_.p, udiag_.p, order_.p,
                                                                         sw_off_.p, A.nb, sw_row_.p, sw_col_.p,
                                                                         sw_val_.p, sw_diag_.p);
     PFG_CUDA(cudaGetLastError());
+    // backward solve (ILUCRS with RHS): levels of the upper dependencies
+    // (row I waits for the rows J > I it stores) and the same layout of its
+    // blocks J > I
+    {
+        std::vector<int> ulvl((size_t)A.nb);
+        int nu = 0;
+        for (int64_t I = A.nb - 1; I >= 0; --I) {
+            int L = 0;
+            for (int64_t q = rp[I]; q < rp[I + 1]; ++q)
+                if (col[q] > I) L = std::max(L, ulvl[col[q]] + 1);
+            ulvl[I] = L;
+            nu = std::max(nu, L + 1);
+        }
+        uptr_.assign((size_t)nu + 1, 0);
+        for (int64_t I = 0; I < A.nb; ++I) ++uptr_[(size_t)ulvl[I] + 1];
+        for (int L = 0; L < nu; ++L) uptr_[L + 1] += uptr_[L];
+        std::vector<int> uorder((size_t)A.nb);
+        std::vector<int64_t> fill(uptr_.begin(), uptr_.end() - 1);
+        for (int64_t I = A.nb - 1; I >= 0; --I) uorder[(size_t)fill[ulvl[I]]++] = (int)I;
+        std::vector<int64_t> uoff((size_t)A.nb + 1, 0);
+        for (int64_t q = 0; q < A.nb; ++q) {
+            const int I = uorder[(size_t)q];
+            int m = 0;
+            for (int64_t k = rp[I]; k < rp[I + 1]; ++k) m += col[k] > I;
+            uoff[(size_t)q + 1] = uoff[(size_t)q] + m;
+        }
+        const int64_t nup = uoff[(size_t)A.nb];
+        uorder_.resize((size_t)A.nb);
+        su_off_.resize((size_t)A.nb + 1);
+        su_row_.resize((size_t)A.nb);
+        su_col_.resize((size_t)std::max<int64_t>(nup, 1));
+        su_val_.resize((size_t)std::max<int64_t>(nup * A.bs * A.bs, 1));
+        su_diag_.resize((size_t)A.nb * (A.bs == 3 ? 8 : 1));
+        PFG_CUDA(cudaMemcpyAsync(uorder_.p, uorder.data(), uorder.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+        PFG_CUDA(cudaMemcpyAsync(su_off_.p, uoff.data(), uoff.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        PFG_CUDA(cudaMemsetAsync(su_diag_.p, 0, su_diag_.bytes(), st));
+        if (A.bs == 3)
+            k_ilu_sweep_layout<3, true><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(
+                A.rp.p, A.col.p, lu_.p, udiag_.p, uorder_.p, su_off_.p, A.nb, su_row_.p, su_col_.p, su_val_.p,
+                su_diag_.p);
+        else
+            k_ilu_sweep_layout<1, true><<<ilu_grid(A.nb), 32 * kIluWarps, 0, st>>>(
+                A.rp.p, A.col.p, lu_.p, udiag_.p, uorder_.p, su_off_.p, A.nb, su_row_.p, su_col_.p, su_val_.p,
+                su_diag_.p);
+        PFG_CUDA(cudaGetLastError());
+    }
     PFG_CUDA(cudaStreamSynchronize(st));
     sweep_bytes_ = (double)nlow * (A.bs * A.bs * 8.0 + 4.0) +
                    (double)A.nb * (8.0 + 8.0 + 8.0 * (A.bs == 3 ? 8 : 1)) + 4.0 * (double)n * 8.0;
@@ -431,6 +594,24 @@ void Ilu0::factor(const DevMatrix &A, bool sorted, cudaStream_t st)
     sorted_ = sorted;
     ++gen_;
     ready_ = true;
+}
+
+void Ilu0::solve(const double *rhs, double *x, cudaStream_t st) const
+{
+    apply(rhs, x, nullptr, st);  // x = D'^-1 L^-1 rhs (D' = U's diagonal, 0 read as 1)
+    const int nu = (int)uptr_.size() - 1;
+    for (int L = 0; L < nu; ++L) {
+        const int64_t cnt = uptr_[L + 1] - uptr_[L];
+        const bool early = L > 0 && cnt <= kIluEarlyRows;
+        const int grid = (int)((cnt + kSweepRows - 1) / kSweepRows);
+        if (bs_ == 3)
+            launch_upper<3>(grid, early, su_row_.p, su_off_.p, su_col_.p, su_val_.p, su_diag_.p, uptr_[L], (int)cnt,
+                            x, st);
+        else
+            launch_upper<1>(grid, early, su_row_.p, su_off_.p, su_col_.p, su_val_.p, su_diag_.p, uptr_[L], (int)cnt,
+                            x, st);
+    }
+    PFG_CUDA(cudaGetLastError());
 }
 
 int Ilu0::apply(const double *v, double *out, const KState *S, cudaStream_t st) const

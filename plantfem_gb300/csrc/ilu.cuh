@@ -46,6 +46,10 @@ class Ilu0 {
     // out = D^-1 L^-1 v on st, one launch per level; the launches return at
     // entry once S says the solve is done (S may be null).  Returns the count.
     int apply(const double *v, double *out, const KState *S, cudaStream_t st) const;
+    // x = the solve of ILUCRS(0, RHS) (SparseClass.f90:1647-1679) with this
+    // factor: the forward sweep above, then the backward substitution with U
+    // (one launch per level of the upper dependencies).  rhs and x distinct.
+    void solve(const double *rhs, double *x, cudaStream_t st) const;
     // Factor values in the matrix's block-row layout and the U diagonal.
     const double *lu() const { return lu_.p; }
     const double *udiag() const { return udiag_.p; }
@@ -71,6 +75,13 @@ class Ilu0 {
     DevBuf<int64_t> sw_off_;
     DevBuf<int> sw_col_;
     DevBuf<double> sw_val_, sw_diag_;
+    // the same for the backward solve: rows by levels of their blocks J > I
+    std::vector<int64_t> uptr_;
+    DevBuf<int> uorder_;
+    DevBuf<int2> su_row_;
+    DevBuf<int64_t> su_off_;
+    DevBuf<int> su_col_;
+    DevBuf<double> su_val_, su_diag_;
     std::vector<int64_t> lptr_;   // level L holds order_[lptr_[L] .. lptr_[L+1])
 };
 

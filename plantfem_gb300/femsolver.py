@@ -228,9 +228,17 @@ class FEMSolver:
         self.last_info = info.as_dict()
         return x
 
-    def ILU(self, sorted: bool = False) -> np.ndarray:
+    def ILU(self, sorted: bool = False, RHS=None) -> np.ndarray:
         """ILUCRS(0) (SparseClass.f90:1629-1792) of the stored matrix, kept on the
-        solver for ILU solves -> the factor's values on getCRS()'s pattern."""
+        solver for ILU solves -> the factor's values on getCRS()'s pattern.
+        With RHS: CRS_%ILU(0, RHS) -> the solve L U x = RHS with the factor
+        (:1647-1679); the stored matrix itself is not overwritten."""
+        if RHS is not None:
+            N.check(self._lib.pfg_ilu_factor(self._h, int(bool(sorted)), None))
+            r = _f64(RHS)
+            x = np.zeros_like(r)
+            N.check(self._lib.pfg_ilu_solve(self._h, N.ptr(r), N.ptr(x)))
+            return x
         lu = np.zeros(self._nnz())
         N.check(self._lib.pfg_ilu_factor(self._h, int(bool(sorted)), N.ptr(lu)))
         return lu

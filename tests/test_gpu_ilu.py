@@ -205,6 +205,35 @@ def test_ilu_apply_uses_the_held_factor(cuda):
     assert np.array_equal(s.ILU(sorted=False), lu)
 
 
+def test_ilu_rhs_solve(cuda):
+    """CRS_%ILU(0, RHS) (Tutorial/std/CRS_test.f90:90-94: [0.54, -0.35, 0.20]),
+    a dense system (ILU(0) = LU: exact), and an FEM system against the oracle's
+    restatement with the same factor."""
+    s = FEMSolver()
+    s.setCRS(CRS=_dense_crs(np.array([[5, 6, 7], [10, 20, 23], [15, 50, 67]], float)))
+    np.testing.assert_allclose(s.ILU(RHS=[2.0, 3.0, 4.0]), [0.54, -0.35, 0.20], rtol=0, atol=1e-13)
+    rng = np.random.default_rng(8)
+    B = rng.standard_normal((10, 10)) + 10 * np.eye(10)
+    t = FEMSolver()
+    t.setCRS(CRS=_dense_crs(B))
+    b = rng.standard_normal(10)
+    np.testing.assert_allclose(t.ILU(RHS=b), np.linalg.solve(B, b), rtol=1e-11)
+    for sys_ in ("fem", "scalar"):
+        if sys_ == "fem":
+            u, p = _fem(4)
+            u.eliminate()
+            rp, ci, _, _ = _oracle_system(p)
+        else:
+            rp, ci, val = _scalar_matrix(60, 11)
+            u = FEMSolver()
+            u.setCRS(CRS=(rp, ci, val))
+        lu = u.ILU(sorted=True)
+        r = rng.standard_normal(rp.shape[0] - 1)
+        x = u.ILU(sorted=True, RHS=r)
+        ref = O.ilu_solve(rp, ci, lu, r)
+        assert np.abs(x - ref).max() <= 1e-11 * np.abs(ref).max(), sys_
+
+
 def test_ilu_refuses_cg_and_mixed(cuda):
     s, p = _fem(3)
     s.eliminate()

@@ -226,6 +226,21 @@ def test_ilu0_tutorial_kats(sorted_):
     assert np.array_equal(O.ilu0(rp, ci, v, sorted_).reshape(3, 3), F3)
 
 
+def test_ilu_rhs_solve_tutorial_kat():
+    """Tutorial/std/CRS_test.f90:90-94: ILU(0, RHS=[2, 3, 4]) of the 3x3 matrix
+    gives [0.54, -0.35, 0.20]; on a dense pattern ILU(0) is the LU factor, so
+    the ILU solve is exact for any right-hand side."""
+    A = np.array([[5, 6, 7], [10, 20, 23], [15, 50, 67]], float)
+    rp, ci, v = _dense_crs(A)
+    lu = O.ilu0(rp, ci, v)
+    np.testing.assert_allclose(O.ilu_solve(rp, ci, lu, [2.0, 3.0, 4.0]), [0.54, -0.35, 0.20], rtol=0, atol=1e-14)
+    rng = np.random.default_rng(6)
+    B = rng.standard_normal((7, 7)) + 7 * np.eye(7)
+    rp, ci, v = _dense_crs(B)
+    b = rng.standard_normal(7)
+    np.testing.assert_allclose(O.ilu_solve(rp, ci, O.ilu0(rp, ci, v), b), np.linalg.solve(B, b), rtol=1e-12)
+
+
 def test_pbicgstab_ilu_tutorial_kat():
     """Tutorial/std/PBiCGSTAB_ILU.f90: x = [0.54, -0.35, 0.20] for the 3x3
     system, er = relative_er = 1e-13."""
