@@ -192,6 +192,114 @@ class FEMDomain:
         self.elemnod = np.array(sel, dtype=np.int32).reshape(len(sel), nne)
         return self
 
+    # ------------------------------------------------ domain decomposition
+    def centerPosition(self, ElementID: int | None = None) -> np.ndarray:
+        """centerPositionFEMDomain (FEMDomainClass.f90:9879 onwards): the mean of the
+        element's node coordinates (ElementID 1-based); all elements' when None."""
+        en = self.elemnod - 1
+        c = np.zeros((self.ne(), 3))
+        for a in range(en.shape[1]):  # sum, then scale, as the reference
+            c = c + self.nodcoord[en[:, a]]
+        c = (1.0 / en.shape[1]) * c
+        return c if ElementID is None else c[int(ElementID) - 1]
+
+    def divide(self, n: int, seed: int | None = None, centers=None) -> list["FEMDomain"]:
+        """FEMDomain_%divide(n) (divide_nFEMDomain, FEMDomainClass.f90:1077-1296):
+        n element "kernels" are drawn, every element goes to the kernel whose centre
+        is nearest (squared distance, the first on ties), and each piece gets
+        ``mpi_global_node_idx`` (its nodes' 1-based global ids, ascending; local
+        node j is global node mpi_global_node_idx[j-1]), local coordinates and
+        connectivity, and ``mpi_shared_node_info`` rows (local node, other piece
+        (0-based), that piece's local node) for the nodes shared with each other
+        piece in piece order.  The reference draws the kernels with an unseeded
+        generator; here ``seed`` seeds the draw, or ``centers`` gives the n
+        kernel element ids (1-based)."""
+        if n == 1:
+            return [self]
+        ne = self.ne()
+        if centers is None:
+            centers = np.random.default_rng(seed).choice(ne, size=n, replace=False) + 1
+        centers = np.asarray(centers, dtype=np.int64)
+        cen = self.centerPosition()
+        cc = cen[centers - 1]
+        d = cen[:, None, :] - cc[None, :, :]
+        norms = d[:, :, 0] * d[:, :, 0] + d[:, :, 1] * d[:, :, 1] + d[:, :, 2] * d[:, :, 2]
+        sub = np.argmin(norms, axis=1)
+        pieces, g2ls = [], []
+        for i in range(n):
+            en = self.elemnod[sub == i]
+            gidx = np.unique(en).astype(np.int32)
+            g2l = np.zeros(self.nn() + 1, dtype=np.int32)
+            g2l[gidx] = np.arange(1, gidx.shape[0] + 1, dtype=np.int32)
+            part = FEMDomain()
+            part.nodcoord = self.nodcoord[gidx - 1].copy()
+            part.elemnod = g2l[en].astype(np.int32)
+            part.mpi_global_node_idx = gidx
+            pieces.append(part)
+            g2ls.append(g2l)
+        for i in range(n):
+            rows = []
+            for j in range(n):
+                if i == j:
+                    continue
+                shared = np.intersect1d(pieces[i].mpi_global_node_idx, pieces[j].mpi_global_node_idx)
+                if shared.shape[0] == 0:
+                    continue
+                rows.append(np.stack([g2ls[i][shared], np.full(shared.shape[0], j, np.int32), g2ls[j][shared]],
+                                     axis=1))
+            pieces[i].mpi_shared_node_info = (np.concatenate(rows).astype(np.int32) if rows
+                                              else np.zeros((0, 3), np.int32))
+        return pieces
+
+    _MPI_CSV_HEADER = ("# number of global node, number of local node, number of shared node,"
+                       "                        number of division ")
+
+    def vtk_MPI(self, name: str, num_division: int, seed: int | None = None, centers=None) -> list[str]:
+        """FEMDomain_%vtk(name, num_division) (vtk_MPI_FEMDOmain, FEMDomainClass.f90:8309-8360):
+        divide the domain and write, for piece i, ``name_<i:06d>.vtk`` and
+        ``name_<i:06d>.csv`` (global and local node counts, its shared-node count
+        and the number of pieces; the local-to-global node map; the shared-node
+        rows).  Returns the written paths."""
+        nn = self.nn()
+        paths = []
+        for i, part in enumerate(self.divide(num_division, seed=seed, centers=centers)):
+            stem = f"{name}_{i:06d}"
+            paths.append(part.vtk(stem))
+            info = part.mpi_shared_node_info
+            lines = [self._MPI_CSV_HEADER,
+                     f"{nn} ,{part.nn()} ,{info.shape[0]} ,{num_division}",
+                     "# local node Idx, global node Idx "]
+            lines += [f"{j + 1} ,{g}" for j, g in enumerate(part.mpi_global_node_idx)]
+            lines.append("# local node Idx, domain Idx, shared local node Idx ")
+            lines += [f"{a} ,{b} ,{c}" for a, b, c in info]
+            with open(stem + ".csv", "w") as f:
+                f.write("\n".join(lines) + "\n")
+            paths.append(stem + ".csv")
+        return paths
+
+    def read_mpi_property(self, name: str) -> int:
+        """read_mpi_propertyFEMDomain (FEMDomainClass.f90:16472-16502): the node map
+        and shared-node rows of a piece -> the number of pieces."""
+        with open(name) as f:
+            lines = [ln.strip() for ln in f if ln.strip()]
+        counts = [int(t) for t in lines[1].replace(",", " ").split()]
+        _, n_loc, n_shared, n_div = counts[:4]
+        self.mpi_global_node_idx = np.zeros(n_loc, dtype=np.int32)
+        for ln in lines[3:3 + n_loc]:
+            idx, val = (int(t) for t in ln.replace(",", " ").split()[:2])
+            self.mpi_global_node_idx[idx - 1] = val
+        rows = [[int(t) for t in ln.replace(",", " ").split()[:3]] for ln in lines[4 + n_loc:4 + n_loc + n_shared]]
+        self.mpi_shared_node_info = np.array(rows, dtype=np.int32).reshape(n_shared, 3)
+        return n_div
+
+    def read_vtk(self, name: str, myrank: int) -> "FEMDomain":
+        """read_vtk (read_vtk_domain_decomposed_FEMDOmain, FEMDomainClass.f90:16505-16513):
+        piece ``myrank`` written by vtk_MPI.  The reference reads
+        ``Cube3D_<rank>`` whatever name it is given; here the name is used."""
+        self.importVTKFile(f"{name}_{int(myrank):06d}.vtk")
+        self.read_mpi_property(f"{name}_{int(myrank):06d}.csv")
+        return self
+
     def deform(self, disp) -> "FEMDomain":
         """nodcoord += reshape(disp, nn, nd) with plantFEM's row-major reshape
         (FEMDomainClass.f90:14482, ArrayClass.f90:5328-5344)."""

@@ -61,3 +61,65 @@ def test_vtk_import_round_trip_and_mixed_cells(tmp_path):
     m = FEMDomain().importVTKFile(str(tmp_path / "mx.vtk"))
     assert m.nn() == 9 and m.elemnod.tolist() == [[1, 2, 3, 4, 5, 6, 7, 8]]
     assert np.array_equal(m.nodcoord[8], [2.0, 0.0, 0.0])
+
+
+def test_divide_known_answer_and_properties():
+    """FEMDomain_%divide (divide_nFEMDomain, FEMDomainClass.f90:1077-1296): a 2x1x1
+    cube split at its two elements shares the middle face; on a larger mesh the
+    pieces partition the elements, each element lies nearest its own kernel,
+    local and global numbering agree and the shared-node rows pair up."""
+    from plantfem_gb300 import FEMDomain
+    d = FEMDomain().create("Cube3D", 2, 1, 1)
+    a, b = d.divide(2, centers=[1, 2])
+    assert a.mpi_global_node_idx.tolist() == [1, 2, 4, 5, 7, 8, 10, 11]
+    assert b.mpi_global_node_idx.tolist() == [2, 3, 5, 6, 8, 9, 11, 12]
+    assert a.mpi_shared_node_info.tolist() == [[2, 1, 1], [4, 1, 3], [6, 1, 5], [8, 1, 7]]
+    assert b.mpi_shared_node_info.tolist() == [[1, 0, 2], [3, 0, 4], [5, 0, 6], [7, 0, 8]]
+
+    big = FEMDomain().create("Cube3D", 6, 5, 4)
+    ps = big.divide(4, seed=3)
+    assert sum(p.ne() for p in ps) == big.ne()
+    # nearest kernel: the element centres of piece i are closest to kernel i
+    kern = np.random.default_rng(3).choice(big.ne(), size=4, replace=False) + 1
+    kc = big.centerPosition()[kern - 1]
+    for i, p in enumerate(ps):
+        pc = p.centerPosition()
+        dist = ((pc[:, None, :] - kc[None, :, :]) ** 2).sum(axis=2)
+        assert np.all(dist[:, i] <= dist.min(axis=1))
+    rows = np.concatenate([p.mpi_global_node_idx[p.elemnod - 1] for p in ps])
+    assert sorted(map(tuple, rows)) == sorted(map(tuple, big.elemnod))
+    for i, p in enumerate(ps):
+        g = p.mpi_global_node_idx
+        assert np.all(np.diff(g) > 0)
+        assert np.array_equal(p.nodcoord, big.nodcoord[g - 1])
+        for loc, j, other in p.mpi_shared_node_info:
+            assert g[loc - 1] == ps[j].mpi_global_node_idx[other - 1]
+            assert [other, i, loc] in ps[j].mpi_shared_node_info.tolist()
+    # every node used by two pieces is listed as shared
+    owners = {}
+    for i, p in enumerate(ps):
+        for gnode in p.mpi_global_node_idx:
+            owners.setdefault(int(gnode), set()).add(i)
+    for i, p in enumerate(ps):
+        listed = {int(p.mpi_global_node_idx[loc - 1]) for loc, _, _ in p.mpi_shared_node_info}
+        assert listed == {gn for gn in map(int, p.mpi_global_node_idx) if len(owners[gn]) > 1}
+
+
+def test_vtk_mpi_round_trip(tmp_path):
+    """vtk_MPI_FEMDOmain (FEMDomainClass.f90:8309-8360) writes each piece's VTK file
+    and node-map CSV; read_vtk (:16505-16513) reads a piece back."""
+    from plantfem_gb300 import FEMDomain
+    d = FEMDomain().create("Cube3D", 4, 3, 3)
+    name = str(tmp_path / "Cube3D")
+    paths = d.vtk_MPI(name, 3, seed=1)
+    assert len(paths) == 6
+    txt = open(name + "_000001.csv").read().splitlines()
+    assert txt[0].startswith("# number of global node, number of local node, number of shared node,")
+    assert txt[1].split(",")[0].strip() == str(d.nn()) and txt[1].split(",")[3].strip() == "3"
+    ref = d.divide(3, seed=1)
+    for rank in range(3):
+        back = FEMDomain().read_vtk(name, rank)
+        assert np.array_equal(back.elemnod, ref[rank].elemnod)
+        assert np.array_equal(back.nodcoord, ref[rank].nodcoord)
+        assert np.array_equal(back.mpi_global_node_idx, ref[rank].mpi_global_node_idx)
+        assert np.array_equal(back.mpi_shared_node_info, ref[rank].mpi_shared_node_info)
