@@ -58,3 +58,40 @@ def test_version_and_defaults_without_gpu(lib):
     # the reference's FEMSolver_ defaults (FEMSolverClass.f90:69-71)
     assert o.itrmax == 100000 and o.er0 == 1e-10 and o.relative_er == 1e-10
     assert o.algorithm == _native.ALG_BICGSTAB and o.precision == _native.PREC_FP64
+
+
+def _header_struct_fields(name):
+    """(type, field) pairs of `typedef struct <name> {...}` in include/pfg.h, in order."""
+    import re
+    txt = open(HEADER).read()
+    body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), txt, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    out = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        parts = decl.split()
+        ctype, names = parts[0], " ".join(parts[1:])
+        for nm in names.split(","):
+            out.append((ctype, nm.strip()))
+    return out
+
+
+@pytest.mark.parametrize("cname,pyname", [("pfg_solve_opts", "SolveOpts"), ("pfg_info", "Info"),
+                                          ("pfg_eig_opts", "EigOpts"), ("pfg_newmark_params", "NewmarkParams"),
+                                          ("pfg_batch_config", "BatchConfig"), ("pfg_batch_info", "BatchInfo")])
+def test_ctypes_structs_match_header(cname, pyname):
+    """Every struct the Python layer passes by pointer has the header's fields in
+    the header's order, with matching C types."""
+    import ctypes as C
+    from plantfem_gb300 import _native as N
+    sizes = {"int32_t": C.c_int32, "int64_t": C.c_int64, "uint64_t": C.c_uint64, "double": C.c_double}
+    hdr = _header_struct_fields(cname)
+    fields = getattr(N, pyname)._fields_
+    assert len(hdr) == len(fields), (cname, hdr, fields)
+    for (ctype, name), (pyfield, pytype) in zip(hdr, fields):
+        assert name.lower() == pyfield.lower() or name.replace("_", "").lower() == pyfield.replace("_", "").lower(), \
+            (cname, name, pyfield)
+        if ctype in sizes:
+            assert C.sizeof(pytype) == C.sizeof(sizes[ctype]), (cname, name)
