@@ -267,11 +267,14 @@ int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *
 
 /* ------------------------------------------------ reference-signature plug-ins */
 /* crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector, n, col_size)
- * (SparseClass-c.c:131-143, bound at SparseClass.f90:38-51): new_vector += A *
- * old_vector on the GPU; host arrays, 1-based row_ptr/col_idx. */
+ * (SparseClass-c.c:53-65, bound at SparseClass.f90:38-51): new_vector += A *
+ * old_vector on the GPU; host arrays, 1-based row_ptr/col_idx.  The argument
+ * list is the reference's, but the reference binds a void C function as a
+ * Fortran subroutine while these return an int status: the Fortran interface
+ * block declares them as integer(c_int) functions (rewritten, not renamed). */
 int pfg_crs_spmv_real64(const double *val, const int64_t *row_ptr, const int32_t *col_idx,
                         const double *old_vector, double *new_vector, size_t n, size_t col_size);
-/* crs_spmv_real32 (SparseClass-c.c:116-128, bound at SparseClass.f90:25-36). */
+/* crs_spmv_real32 (SparseClass-c.c:38-50, bound at SparseClass.f90:25-36). */
 int pfg_crs_spmv_real32(const float *val, const int64_t *row_ptr, const int32_t *col_idx,
                         const float *old_vector, float *new_vector, size_t n, size_t col_size);
 
@@ -289,14 +292,20 @@ int pfg_linear_solver_crs(const int64_t *row_ptr, const int32_t *col_idx, const 
  * arrays, rhs and x (x0 on entry, solution on exit) in DEVICE memory; this
  * call allocates nothing -- no cudaMalloc, cudaFree or allocating library
  * routine.  Its work vectors and reduction scratch live in one static device
- * array sized for at most 262,144 unknowns (about 10.5 MB, held on every GPU
- * that loads the library until the process exits); larger n is rejected with
- * PFG_E_ARG.  FP64 conjugate gradients only, point Jacobi or no
- * preconditioner (opts NULL: CG + Jacobi, true relative residual 1e-10).
- * The first call on a device looks up the array's device address, so make it
- * before any stream capture.  Every call shares the one array (calls are
- * serialised and each returns after its stream has finished): work from
- * other callers that overlaps it on the GPU would race.  stream may be NULL. */
+ * array sized for at most 262,144 unknowns (about 10.5 MB); larger n is
+ * rejected with PFG_E_ARG.  CUDA loads that array (with this entry point's
+ * kernels) on a device the first time the entry point runs there, because
+ * modules load lazily by default, and keeps it until the process exits.  So a
+ * caller that must not allocate during its solves makes one set-up call per
+ * device first -- n = 0, every pointer may be NULL, nothing is solved -- with
+ * that device current and before any stream capture, or runs with
+ * CUDA_MODULE_LOADING=EAGER.  FP64 conjugate gradients only, point Jacobi or
+ * no preconditioner, stop rule PFG_STOP_TRUE_RELATIVE only (others return
+ * PFG_E_UNSUPPORTED; opts NULL: CG + Jacobi, true relative residual 1e-10).
+ * Every call shares the one array and finds the previous call's contents in
+ * it (the solver clears what must start at zero); calls are serialised and
+ * each returns after its stream has finished, but work from another caller
+ * that overlaps it on the GPU would race.  stream may be NULL. */
 int pfg_linear_solver_crs_noalloc(const int64_t *d_row_ptr, const int32_t *d_col_idx, const double *d_val,
                                   const double *d_rhs, double *d_x, int64_t n, const pfg_solve_opts *opts,
                                   pfg_info *info, void *stream);

@@ -31,13 +31,20 @@ _u8 = np.ctypeslib.ndpointer(dtype=np.uint8, flags="C_CONTIGUOUS")
 
 
 def build(with_ref: bool | None = None) -> None:
-    """Compile liboracle.so (and oracle/_ref when the reference checkout exists)."""
-    targets = ["all"]
-    if with_ref is None:
-        with_ref = os.path.exists("/root/reference/src/SparseClass/SparseClass-c.c")
-    if with_ref:
-        targets.append("ref")
-    subprocess.run(["make", "-s", "-C", _HERE] + targets, check=True)
+    """Compile liboracle.so, and oracle/_ref from the plantFEM checkout.
+
+    The checkout's location comes from the ``PLANTFEM_SRC`` environment
+    variable (default in ``oracle/Makefile``).  ``with_ref=None`` builds
+    ``_ref`` only where that checkout exists (the make target fails quietly
+    otherwise); ``True`` requires it; ``False`` skips it.
+    """
+    subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
+    if with_ref is False:
+        return
+    r = subprocess.run(["make", "-s", "-C", _HERE, "ref"], stdout=subprocess.DEVNULL,
+                       stderr=None if with_ref else subprocess.DEVNULL)
+    if with_ref and r.returncode != 0:
+        raise RuntimeError("oracle/_ref: the plantFEM checkout named by PLANTFEM_SRC is missing")
 
 
 def lib():
@@ -228,7 +235,7 @@ def spmv(row_ptr, col_idx, val, x, atomic=False):
 
 
 def crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector):
-    """Restated SparseClass-c.c:131-143 (accumulates into new_vector)."""
+    """Restated SparseClass-c.c:53-65 (accumulates into new_vector)."""
     lib().orc_crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector, new_vector.shape[0],
                               col_idx.shape[0])
 

@@ -15,7 +15,7 @@
  *   - element matrices are 24x24 column-major, local DOF = 3*(a-1)+d.
  *
  * Pinning: orc_crs_spmv_real64 is checked bit-for-bit against the reference's
- * own C SpMV (src/SparseClass/SparseClass-c.c:131-143) compiled into
+ * own C SpMV (src/SparseClass/SparseClass-c.c:53-65) compiled into
  * oracle/_ref; the pattern builders are checked against each other the way
  * Tutorial/fem/CRS_Zero_Matrix.f90:10-29 does; the full solve path is checked
  * against the gravity-bar known answer of
@@ -559,7 +559,7 @@ void orc_apply_fix(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, do
 /* ------------------------------------------------------------------------ */
 /* A14/A15 SpMV                                                                */
 /* ------------------------------------------------------------------------ */
-/* crs_spmv_real64 restated (SparseClass-c.c:131-143): accumulates
+/* crs_spmv_real64 restated (SparseClass-c.c:53-65): accumulates
  * new_vector[row] += val*old_vector[col]; row_ptr/col_idx 1-based. */
 void orc_crs_spmv_real64(const double *val, const int64_t *row_ptr, const int32_t *col_idx,
                          const double *old_vector, double *new_vector, size_t n, size_t col_size)

@@ -32,7 +32,12 @@ def read_crs_files(name: str):
 
 
 def write_dense_csv(path: str, row_ptr, col_idx, val, zero_or_nonzero: bool = False, max_n: int = 20000) -> None:
-    """CRS_as_dense: the matrix as an n x n CSV (or '0' / '*' per entry)."""
+    """CRS_as_dense: the matrix as an n x n CSV.
+
+    With ``zero_or_nonzero`` each entry is one character, ``0`` or ``*``, with
+    no separator between them, as FEMSolverClass.f90:1265-1285 writes it (its
+    ``cycle`` skips the comma).
+    """
     n = len(row_ptr) - 1
     if n > max_n:
         raise ValueError(f"dense CSV of a {n} x {n} matrix refused (limit {max_n})")
@@ -42,6 +47,6 @@ def write_dense_csv(path: str, row_ptr, col_idx, val, zero_or_nonzero: bool = Fa
             lo, hi = row_ptr[i] - 1, row_ptr[i + 1] - 1
             row[np.asarray(col_idx[lo:hi]) - 1] = val[lo:hi]
             if zero_or_nonzero:
-                f.write(",".join("0" if x == 0.0 else "*" for x in row) + "\n")
+                f.write("".join("0" if x == 0.0 else "*" for x in row) + "\n")
             else:
                 f.write(",".join(repr(float(x)) for x in row) + "\n")

@@ -572,7 +572,7 @@ int crs_spmv_host(const T *val, const int64_t *row_ptr, const int32_t *col_idx, 
         std::vector<T> hy(n);
         PFG_CUDA(cudaMemcpyAsync(hy.data(), y.p, n * sizeof(T), cudaMemcpyDeviceToHost, st));
         PFG_CUDA(cudaStreamSynchronize(st));
-        // SparseClass-c.c:139-141 accumulates into new_vector
+        // SparseClass-c.c:61-63 accumulates into new_vector
         for (size_t i = 0; i < n; ++i) new_vector[i] = new_vector[i] + hy[i];
     });
 }

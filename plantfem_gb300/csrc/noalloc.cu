@@ -6,8 +6,12 @@
 // code that must not call cudaMalloc/cudaFree while other work is queued.  The
 // caller passes the CRS matrix, right-hand side and solution in device memory;
 // every work vector, the reduction partials and the solver scalars live in
-// one file-scope __device__ array of fixed size (kNaMaxDof DOF), which every
-// GPU that loads the library keeps until the process exits.
+// one file-scope __device__ array of fixed size (kNaMaxDof DOF).  CUDA loads
+// this file's module, and with it the array, on a device the first time the
+// entry point runs there (lazy module loading, the default), and the device
+// keeps it until the process exits.  Callers that must not allocate at all
+// while they solve make one set-up call (n = 0) per device first, or run with
+// CUDA_MODULE_LOADING=EAGER, which loads every module when the context is made.
 #include <chrono>
 #include <cmath>
 #include <mutex>
@@ -142,21 +146,16 @@ __global__ void __launch_bounds__(kNaThreads)
     }
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array on the current device.  Looked up on
+// every call rather than cached: after a context reset the module is loaded
+// again at another address, and once the module is loaded the lookup itself
+// allocates nothing.  The first lookup on a device is what loads this file's
+// module there (CUDA loads modules lazily by default), placing the array.
 static double *scratch_address()
 {
-    static std::mutex mu;
-    static double *addr[64] = {nullptr};
-    int dev = 0;
-    PFG_CUDA(cudaGetDevice(&dev));
-    PFG_CHECK(dev >= 0 && dev < 64, PFG_E_UNSUPPORTED, "device ordinal above 63");
-    std::lock_guard<std::mutex> lk(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        PFG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        addr[dev] = (double *)p;
-    }
-    return addr[dev];
+    void *p = nullptr;
+    PFG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    return (double *)p;
 }
 
 }  // namespace pfg
@@ -171,8 +170,13 @@ extern "C" int pfg_linear_solver_crs_noalloc(const int64_t *d_row_ptr, const int
     int status = PFG_OK;
     NaState h{};
     const int rc = guard([&] {
+        PFG_CHECK(n >= 0, PFG_E_ARG, "n must not be negative");
+        if (n == 0) {  // set-up only: load the module and place the array on this device
+            std::lock_guard<std::mutex> lk(call_mu);
+            (void)scratch_address();
+            return;
+        }
         PFG_CHECK(d_row_ptr && d_col_idx && d_val && d_rhs && d_x, PFG_E_ARG, "NULL argument");
-        PFG_CHECK(n > 0, PFG_E_ARG, "n must be positive");
         PFG_CHECK(n <= kNaMaxDof, PFG_E_ARG,
                   "pfg_linear_solver_crs_noalloc: n = " + std::to_string(n) + " exceeds the static scratch limit of " +
                       std::to_string(kNaMaxDof) + " DOF; use pfg_linear_solver_crs");
@@ -186,6 +190,8 @@ extern "C" int pfg_linear_solver_crs_noalloc(const int64_t *d_row_ptr, const int
                   "pfg_linear_solver_crs_noalloc: FP64 CG only");
         PFG_CHECK(opts->precond == PFG_PC_NONE || opts->precond == PFG_PC_JACOBI, PFG_E_UNSUPPORTED,
                   "pfg_linear_solver_crs_noalloc: point Jacobi or no preconditioner");
+        PFG_CHECK(opts->stop_rule == PFG_STOP_TRUE_RELATIVE, PFG_E_UNSUPPORTED,
+                  "pfg_linear_solver_crs_noalloc: stop rule PFG_STOP_TRUE_RELATIVE only");
         const double tol = opts->relative_er > 0 ? opts->relative_er : 1e-10;
         const int itrmax = opts->itrmax > 0 ? opts->itrmax : 100000;
         cudaStream_t st = (cudaStream_t)stream;

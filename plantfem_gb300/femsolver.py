@@ -370,7 +370,7 @@ class FEMSolver:
 
 
 def crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector):
-    """GPU crs_spmv_real64 with the reference signature (SparseClass-c.c:131-143):
+    """GPU crs_spmv_real64 with the reference signature (SparseClass-c.c:53-65):
     new_vector += A old_vector, 1-based CRS."""
     lib = N.load()
     v, rp, ci, x = _f64(val), _i64(row_ptr), _i32(col_idx), _f64(old_vector)

@@ -51,7 +51,7 @@ def _random_crs(n, density, seed):
 
 @pytest.mark.skipif(O.ref_lib() is None, reason="reference C SpMV not compiled here (no reference checkout)")
 def test_spmv_bit_exact_vs_reference_c():
-    """orc_crs_spmv_real64 == the reference's crs_spmv_real64 (SparseClass-c.c:131-143), bit for bit."""
+    """orc_crs_spmv_real64 == the reference's crs_spmv_real64 (SparseClass-c.c:53-65), bit for bit."""
     R = O.ref_lib()
     for seed, n in ((0, 1), (1, 37), (2, 1000)):
         rp, ci, val, x = _random_crs(n, 0.05, seed)
