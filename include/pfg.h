@@ -442,9 +442,11 @@ int pfg_batch_abort_flag(pfg_batch *b, volatile int32_t **flag);
  * the upper half of a symmetric matrix (PFG_STORAGE_SYMMETRIC), 8 = its CG form
  * with the fused p.Ap (the dominant kernel of the symmetric-storage mixed CG),
  * 9 = one D^-1 L^-1 sweep of the held ILU(0) factor (all its level launches;
- * the factor is taken in ascending column order first if none is held).
- * Kernels 2, 5, 6 and 8 need a symmetric positive definite (eliminated)
- * matrix, 7 a symmetric one. */
+ * the factor is taken in ascending column order first if none is held),
+ * 10 = the reproducible FP32 symmetric product of the mixed BiCGSTAB (own
+ * blocks in FP32, transposes in 64-bit fixed point; its finish pass is not
+ * part of the launch).  Kernels 2, 5, 6 and 8 need a symmetric positive
+ * definite (eliminated) matrix, 7 and 10 a symmetric one. */
 int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, double *ms_per_launch, double *bytes_per_launch);
 
 #ifdef __cplusplus

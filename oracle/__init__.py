@@ -85,6 +85,7 @@ def lib():
     L.orc_bicgstab_ilu.argtypes = [C.c_int64, _i64, _i32, _d, _d, _d, _d, C.c_int, C.c_double, C.c_double,
                                    C.POINTER(C.c_int)]
     L.orc_num_threads.restype = C.c_int
+    L.orc_crs_spmm.argtypes = [C.c_int64, _i64, _i32, _d, C.c_int64, _d, _d]
     _LIB = L
     return L
 
@@ -286,6 +287,28 @@ def bicgstab_ilu(row_ptr, col_idx, val, b, lu=None, sorted=False, x0=None, itrma
     rc = lib().orc_bicgstab_ilu(n, row_ptr, col_idx, val, lu, x, np.ascontiguousarray(b, dtype=np.float64),
                                 itrmax, er0, relative_er, C.byref(it))
     return x, rc, it.value
+
+
+def spmm(row_ptr, col_idx, val, X):
+    """Y = A X for a block of vectors X (n x m), the oracle's CRS_%matmul per column."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    n = row_ptr.shape[0] - 1
+    Y = np.empty((n, X.shape[1]))
+    lib().orc_crs_spmm(n, row_ptr, col_idx, val, X.shape[1], X.reshape(-1), Y.reshape(-1))
+    return Y
+
+
+class CrsOperator:
+    """A 1-based CRS matrix usable as ``A @ X`` in ``oracle.lobpcg`` (OpenMP products)."""
+
+    def __init__(self, row_ptr, col_idx, val):
+        self.row_ptr, self.col_idx, self.val = row_ptr, col_idx, val
+        self.shape = (row_ptr.shape[0] - 1, row_ptr.shape[0] - 1)
+
+    def __matmul__(self, X):
+        if X.ndim == 1:
+            return spmm(self.row_ptr, self.col_idx, self.val, X[:, None])[:, 0]
+        return spmm(self.row_ptr, self.col_idx, self.val, X)
 
 
 def pcg(row_ptr, col_idx, val, b, tol=1e-12, maxit=200000, x0=None):

@@ -17,7 +17,7 @@ import scipy.linalg as sla
 def gram_schmidt(V: np.ndarray) -> np.ndarray:
     """GramSchmidt (SparseClass.f90:2243-2275): column-sequential modified GS,
     zero columns skipped, each column normalised after projection."""
-    out = V.copy()
+    out = np.asfortranarray(V, dtype=np.float64).copy(order="F")  # contiguous columns
     m = out.shape[1]
     for i in range(m):
         viold = out[:, i].copy()

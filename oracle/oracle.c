@@ -740,6 +740,30 @@ int64_t orc_reduce_crs(int64_t n, const int64_t *row_ptr, const int32_t *col_idx
     return m;
 }
 
+/* CRS_%matmul of a block of vectors (crs_matvec_generic_SparseClass,       */
+/* SparseClass.f90:834-943, applied column by column as LOBPCG_CRS does):     */
+/* Y(i, :) = sum_k val(k) X(col(k), :), X and Y row-major n x m.  Each column */
+/* of Y is the same row sum, in the same order, as orc_sub_crs_matvec's.      */
+void orc_crs_spmm(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, const double *val, int64_t m,
+                  const double *X, double *Y)
+{
+#pragma omp parallel
+    {
+        double *acc = malloc((size_t)m * sizeof(double));
+#pragma omp for schedule(static)
+        for (int64_t row = 0; row < n; ++row) {
+            for (int64_t j = 0; j < m; ++j) acc[j] = 0.0;
+            for (int64_t k = row_ptr[row]; k < row_ptr[row + 1]; ++k) {
+                const double a = val[k - 1];
+                const double *xr = X + (int64_t)(col_idx[k - 1] - 1) * m;
+                for (int64_t j = 0; j < m; ++j) acc[j] = acc[j] + a * xr[j];
+            }
+            for (int64_t j = 0; j < m; ++j) Y[row * m + j] = acc[j];
+        }
+        free(acc);
+    }
+}
+
 int orc_num_threads(void)
 {
 #ifdef _OPENMP

@@ -151,7 +151,7 @@ void build_pattern(const DevMesh &m, DevMatrix &K, cudaStream_t st)
     DevBuf<unsigned long long> cnt((size_t)nn + 1);
     DevBuf<int64_t> eptr((size_t)nn + 1);
     PFG_CUDA(cudaMemsetAsync(cnt.p, 0, (nn + 1) * sizeof(unsigned long long), st));
-    const int g = grid_for(ne * 8, 256, 152 * 16);
+    const int g = grid_for(ne * 8, 256, sm_count_device() * 16);
     k_count_incidence<<<g, 256, 0, st>>>(m.conn.p, ne, cnt.p);
     PFG_CUDA(cudaGetLastError());
     const int64_t ninc = exclusive_scan((const int64_t *)cnt.p, eptr.p, nn + 1, st);
@@ -159,7 +159,7 @@ void build_pattern(const DevMesh &m, DevMatrix &K, cudaStream_t st)
     DevBuf<int> elist((size_t)ninc);
     PFG_CUDA(cudaMemsetAsync(cnt.p, 0, (nn + 1) * sizeof(unsigned long long), st));
     k_fill_incidence<<<g, 256, 0, st>>>(m.conn.p, ne, eptr.p, cnt.p, elist.p);
-    const int gn = grid_for(nn, 128, 152 * 16);
+    const int gn = grid_for(nn, 128, sm_count_device() * 16);
     k_sort_incidence<<<gn, 128, 0, st>>>(nn, eptr.p, elist.p);
     PFG_CUDA(cudaGetLastError());
     DevBuf<int64_t> ncnt((size_t)nn + 1);
@@ -464,7 +464,7 @@ void assemble_elements(const DevMesh &m, DevMatrix &K, int kind, const double *p
     for (size_t c = 0; c + 1 < m.color_ptr.size(); ++c) {
         const int64_t n = m.color_ptr[c + 1] - m.color_ptr[c];
         if (n == 0) continue;
-        const int grid = (int)std::min<int64_t>((n + kEPB - 1) / kEPB, 152 * 16);
+        const int grid = (int)std::min<int64_t>((n + kEPB - 1) / kEPB, sm_count_device() * 16);
         k_element_matrix<<<grid, 64 * kEPB, 0, st>>>(n, m.color_elems.p + m.color_ptr[c], m.xyz.p, m.nn, m.conn.p,
                                                       m.ne, kind, p0, p1, broadcast ? 1 : 0, K.rp.p, K.col.p,
                                                       K.v64.p, 0, nullptr, err.p);
@@ -479,7 +479,7 @@ void element_stiffness(const DevMesh &m, const double *E, const double *nu, bool
 {
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-    const int grid = (int)std::min<int64_t>((m.ne + kEPB - 1) / kEPB, 152 * 16);
+    const int grid = (int)std::min<int64_t>((m.ne + kEPB - 1) / kEPB, sm_count_device() * 16);
     k_element_matrix<<<grid, 64 * kEPB, 0, st>>>(m.ne, nullptr, m.xyz.p, m.nn, m.conn.p, m.ne, 0, E, nu,
                                                   broadcast ? 1 : 0, nullptr, nullptr, nullptr, 1, out, err.p);
     PFG_CUDA(cudaGetLastError());
@@ -532,7 +532,7 @@ void assemble_body_force(const DevMesh &m, double *rhs, const double *rho, bool 
     for (size_t c = 0; c + 1 < m.color_ptr.size(); ++c) {
         const int64_t n = m.color_ptr[c + 1] - m.color_ptr[c];
         if (n == 0) continue;
-        k_body_force<<<grid_for(n, 128, 152 * 16), 128, 0, st>>>(n, m.color_elems.p + m.color_ptr[c], m.xyz.p, m.nn,
+        k_body_force<<<grid_for(n, 128, sm_count_device() * 16), 128, 0, st>>>(n, m.color_elems.p + m.color_ptr[c], m.xyz.p, m.nn,
                                                                  m.conn.p, m.ne, rho, broadcast ? 1 : 0, accel[0],
                                                                  accel[1], accel[2], rhs, err.p);
         PFG_CUDA(cudaGetLastError());
@@ -571,7 +571,7 @@ void scatter_element_matrices(const DevMesh &m, DevMatrix &K, int64_t count, con
     PFG_CHECK(K.bs == 3 && K.nb == m.nn, PFG_E_STATE, "pattern not built for this mesh (call setCRS(DOF=3))");
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-    k_scatter_mats<<<grid_for(count * 64, 256, 152 * 16), 256, 0, st>>>(count, ids, mats, m.conn.p, m.ne, K.rp.p,
+    k_scatter_mats<<<grid_for(count * 64, 256, sm_count_device() * 16), 256, 0, st>>>(count, ids, mats, m.conn.p, m.ne, K.rp.p,
                                                                         K.col.p, K.v64.p, err.p);
     PFG_CUDA(cudaGetLastError());
     K.values_changed();
@@ -601,7 +601,7 @@ void scatter_element_vectors(const DevMesh &m, double *rhs, int64_t count, const
     if (count == 0) return;
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-    k_scatter_vecs<<<grid_for(count * 24, 256, 152 * 16), 256, 0, st>>>(count, ids, vecs, m.conn.p, m.ne, rhs, err.p);
+    k_scatter_vecs<<<grid_for(count * 24, 256, sm_count_device() * 16), 256, 0, st>>>(count, ids, vecs, m.conn.p, m.ne, rhs, err.p);
     PFG_CUDA(cudaGetLastError());
     int h = 0;
     PFG_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -673,7 +673,7 @@ void element_stress(const DevMesh &m, const double *disp, const double *E, const
 {
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-    k_stress<<<grid_for(m.ne, 128, 152 * 16), 128, 0, st>>>(m.ne, m.xyz.p, m.nn, m.conn.p, disp, E, nu,
+    k_stress<<<grid_for(m.ne, 128, sm_count_device() * 16), 128, 0, st>>>(m.ne, m.xyz.p, m.nn, m.conn.p, disp, E, nu,
                                                             broadcast ? 1 : 0, out, err.p);
     PFG_CUDA(cudaGetLastError());
     check_err(err, st);
@@ -721,7 +721,7 @@ void adjoint_grad_E(const DevMesh &m, const double *u, const double *lam, const 
 {
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-    k_adjoint_grad<<<grid_for(m.ne, 128, 152 * 16), 128, 0, st>>>(m.ne, m.xyz.p, m.nn, m.conn.p, u, lam, nu,
+    k_adjoint_grad<<<grid_for(m.ne, 128, sm_count_device() * 16), 128, 0, st>>>(m.ne, m.xyz.p, m.nn, m.conn.p, u, lam, nu,
                                                                   broadcast ? 1 : 0, grad, err.p);
     PFG_CUDA(cudaGetLastError());
     check_err(err, st);
@@ -762,7 +762,7 @@ __global__ void k_dirichlet(int64_t nb, const int64_t *__restrict__ rp, const in
 
 void apply_dirichlet(DevMatrix &K, double *rhs, const uint8_t *fixed, const double *fixval, cudaStream_t st)
 {
-    const int g = grid_for(K.nb, 128, 152 * 16);
+    const int g = grid_for(K.nb, 128, sm_count_device() * 16);
     if (K.bs == 3)
         k_dirichlet<3><<<g, 128, 0, st>>>(K.nb, K.rp.p, K.col.p, K.v64.p, rhs, fixed, fixval);
     else
@@ -779,7 +779,7 @@ __global__ void k_restore_fixed(int64_t n, double *x, const uint8_t *fixed, cons
 
 void restore_fixed(int64_t n, double *x, const uint8_t *fixed, const double *fixval, cudaStream_t st)
 {
-    k_restore_fixed<<<grid_for(n, 256, 152 * 8), 256, 0, st>>>(n, x, fixed, fixval);
+    k_restore_fixed<<<grid_for(n, 256, sm_count_device() * 8), 256, 0, st>>>(n, x, fixed, fixval);
     PFG_CUDA(cudaGetLastError());
 }
 
@@ -866,7 +866,7 @@ void import_crs(int64_t n, int64_t nnz, const int64_t *row_ptr, const int32_t *c
     if (allow_blocks && n % 3 == 0 && val != nullptr) {
         hok = 1;
         PFG_CUDA(cudaMemcpyAsync(ok.p, &hok, sizeof(int), cudaMemcpyHostToDevice, st));
-        k_check_blocks<<<grid_for(n / 3, 256, 152 * 16), 256, 0, st>>>(n / 3, row_ptr, col_idx, n, ok.p);
+        k_check_blocks<<<grid_for(n / 3, 256, sm_count_device() * 16), 256, 0, st>>>(n / 3, row_ptr, col_idx, n, ok.p);
         PFG_CUDA(cudaGetLastError());
         PFG_CUDA(cudaMemcpyAsync(&hok, ok.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         PFG_CUDA(cudaStreamSynchronize(st));
@@ -881,7 +881,7 @@ void import_crs(int64_t n, int64_t nnz, const int64_t *row_ptr, const int32_t *c
         K.rp.resize((size_t)nb + 1);
         K.col.resize((size_t)std::max<int64_t>(K.nnzb, 1));
         K.v64.resize((size_t)std::max<int64_t>(nnz, 1));
-        k_import_b3<<<grid_for(nb, 128, 152 * 16), 128, 0, st>>>(nb, row_ptr, col_idx, val, K.rp.p, K.col.p,
+        k_import_b3<<<grid_for(nb, 128, sm_count_device() * 16), 128, 0, st>>>(nb, row_ptr, col_idx, val, K.rp.p, K.col.p,
                                                                  K.v64.p);
         PFG_CUDA(cudaGetLastError());
     } else {
@@ -893,7 +893,7 @@ void import_crs(int64_t n, int64_t nnz, const int64_t *row_ptr, const int32_t *c
         K.v64.resize((size_t)std::max<int64_t>(nnz, 1));
         int zero = 0;
         PFG_CUDA(cudaMemcpyAsync(ok.p, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-        k_import_b1<<<grid_for(std::max(n + 1, nnz), 256, 152 * 16), 256, 0, st>>>(n, row_ptr, col_idx, nnz, K.rp.p,
+        k_import_b1<<<grid_for(std::max(n + 1, nnz), 256, sm_count_device() * 16), 256, 0, st>>>(n, row_ptr, col_idx, nnz, K.rp.p,
                                                                                    K.col.p, ok.p);
         PFG_CUDA(cudaGetLastError());
         if (nnz && val) PFG_CUDA(cudaMemcpyAsync(K.v64.p, val, nnz * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -939,7 +939,7 @@ __global__ void k_export_b1(int64_t n, int64_t nnz, const int64_t *__restrict__ 
 void export_values(const DevMatrix &K, const double *bval, double *val, cudaStream_t st)
 {
     if (K.bs == 3)
-        k_export_b3<<<grid_for(K.nb, 128, 152 * 16), 128, 0, st>>>(K.nb, K.rp.p, K.col.p, bval, nullptr, nullptr,
+        k_export_b3<<<grid_for(K.nb, 128, sm_count_device() * 16), 128, 0, st>>>(K.nb, K.rp.p, K.col.p, bval, nullptr, nullptr,
                                                                    val);
     else if (K.nnzb)
         PFG_CUDA(cudaMemcpyAsync(val, bval, K.nnzb * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -949,10 +949,10 @@ void export_values(const DevMatrix &K, const double *bval, double *val, cudaStre
 void export_crs(const DevMatrix &K, int64_t *row_ptr, int32_t *col_idx, double *val, cudaStream_t st)
 {
     if (K.bs == 3) {
-        k_export_b3<<<grid_for(K.nb, 128, 152 * 16), 128, 0, st>>>(K.nb, K.rp.p, K.col.p, K.v64.p, row_ptr, col_idx,
+        k_export_b3<<<grid_for(K.nb, 128, sm_count_device() * 16), 128, 0, st>>>(K.nb, K.rp.p, K.col.p, K.v64.p, row_ptr, col_idx,
                                                                    val);
     } else {
-        k_export_b1<<<grid_for(std::max(K.nb + 1, K.nnzb), 256, 152 * 16), 256, 0, st>>>(K.nb, K.nnzb, K.rp.p,
+        k_export_b1<<<grid_for(std::max(K.nb + 1, K.nnzb), 256, sm_count_device() * 16), 256, 0, st>>>(K.nb, K.nnzb, K.rp.p,
                                                                                         K.col.p, row_ptr, col_idx);
         if (val && K.nnzb)
             PFG_CUDA(cudaMemcpyAsync(val, K.v64.p, K.nnzb * sizeof(double), cudaMemcpyDeviceToDevice, st));

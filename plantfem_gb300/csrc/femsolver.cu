@@ -1078,7 +1078,7 @@ int pfg_newmark_setup(pfg_solver *h, const pfg_newmark_params *p)
         const double cK = 1.0 + g / (b * dt) * p->rayleigh_beta;
         copy_matrix(*Kp, h->K, h->st);
         const int64_t len = Kp->nnzb * Kp->bs * Kp->bs;
-        k_combine_values<<<grid_for(len, 256, 152 * 16), 256, 0, h->st>>>(len, cM, Mp->v64.p, cK, Kp->v64.p,
+        k_combine_values<<<grid_for(len, 256, sm_count_device() * 16), 256, 0, h->st>>>(len, cM, Mp->v64.p, cK, Kp->v64.p,
                                                                           h->K.v64.p);
         PFG_CUDA(cudaGetLastError());
         h->K.values_changed();
@@ -1145,7 +1145,7 @@ int pfg_newmark_step(pfg_solver *h, const pfg_solve_opts *opts, int64_t n, const
         const double mu = 1.0 / (b * dt * dt) + nm.ray_alpha * du, mv = 1.0 / (b * dt) + nm.ray_alpha * dv,
                      ma = 1.0 / (2.0 * b) - 1.0 + nm.ray_alpha * da;
         const double ku = nm.ray_beta * du, kv = nm.ray_beta * dv, ka = nm.ray_beta * da;
-        const int gv = grid_for(n, 256, 152 * 16);
+        const int gv = grid_for(n, 256, sm_count_device() * 16);
         if (a_ext) PFG_CUDA(cudaMemcpyAsync(nm.tmp.p, a_ext, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
         k_newmark_weights<<<gv, 256, 0, h->st>>>(n, a_ext ? nm.tmp.p : nullptr, nm.u.p, nm.v.p, nm.a.p, mu, mv, ma,
                                                  ku, kv, ka, nm.wM.p, nm.wK.p);

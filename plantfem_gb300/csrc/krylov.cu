@@ -115,6 +115,25 @@ __device__ __forceinline__ bool grid_total(Comp32 (&v)[NV], double *, float *pf,
 
 __device__ __forceinline__ bool finite_d(double x) { return isfinite(x); }
 
+// *bits = max(*bits, v) for non-negative floats (their bit patterns order as
+// unsigned integers); one atomic per CTA (every thread of the CTA calls this).
+// A non-finite v is kept as +inf.
+__device__ __forceinline__ void track_abs_max(float v, unsigned *bits)
+{
+    __shared__ float wmax[32];
+    if (!(v <= 3.0e38f)) v = __int_as_float(0x7f800000);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) wmax[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = wmax[0];
+        for (int k = 1; k < nw; ++k) m = fmaxf(m, wmax[k]);
+        atomicMax(bits, __float_as_uint(m));
+    }
+}
+
 // ------------------------------------------------------------ plain kernels
 template <int BS, typename T>
 __global__ void __launch_bounds__(kThreads) k_spmv(BsrView<T> A, const T *__restrict__ x, T *__restrict__ y)
@@ -510,6 +529,7 @@ __global__ void __launch_bounds__(kThreads)
             S->rmax32 = sqrtf(tot[1]);
             S->rmin32 = S->rmax32;
             S->need_update = 0;
+            S->xmax_bits = 0u;
         }
     }
 }
@@ -730,12 +750,13 @@ __global__ void __launch_bounds__(kThreads)
 template <int BS, typename T>
 __global__ void __launch_bounds__(kThreads)
     k_bicg_dir(int64_t nb, const T *__restrict__ r, T *__restrict__ p, const T *__restrict__ y, T *__restrict__ ph,
-               const T *__restrict__ dinv, int pc, KState *S)
+               const T *__restrict__ dinv, int pc, KState *S, bool track_max = false)
 {
     if (S->done | S->need_update) return;
     const bool f64 = sizeof(T) == 8;
     const T beta = f64 ? (T)S->beta : (T)S->beta32;
     const T c3 = f64 ? (T)S->c3 : (T)S->c3_32;
+    float vmax = 0.f;
     for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
          row += (int64_t)gridDim.x * blockDim.x) {
         T pv[BS], hv[BS];
@@ -750,16 +771,21 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int i = 0; i < BS; ++i) ph[(int64_t)BS * row + i] = hv[i];
         }
+        if (track_max)
+#pragma unroll
+            for (int i = 0; i < BS; ++i) vmax = fmaxf(vmax, fabsf((float)(pc != PFG_PC_NONE ? hv[i] : pv[i])));
     }
+    if (track_max) track_abs_max(vmax, &S->xmax_bits);
 }
 
 template <int BS, typename T>
 __global__ void __launch_bounds__(kThreads)
     k_bicg_e(int64_t nb, const T *__restrict__ r, const T *__restrict__ y, T *__restrict__ e, T *__restrict__ eh,
-             const T *__restrict__ dinv, int pc, KState *S)
+             const T *__restrict__ dinv, int pc, KState *S, bool track_max = false)
 {
     if (S->done | S->need_update) return;
     const T alpha = sizeof(T) == 8 ? (T)S->alpha : (T)S->alpha32;
+    float vmax = 0.f;
     for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
          row += (int64_t)gridDim.x * blockDim.x) {
         T ev[BS], hv[BS];
@@ -774,7 +800,11 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
             for (int i = 0; i < BS; ++i) eh[(int64_t)BS * row + i] = hv[i];
         }
+        if (track_max)
+#pragma unroll
+            for (int i = 0; i < BS; ++i) vmax = fmaxf(vmax, fabsf((float)(pc != PFG_PC_NONE ? hv[i] : ev[i])));
     }
+    if (track_max) track_abs_max(vmax, &S->xmax_bits);
 }
 
 template <int BS, typename T>
@@ -894,6 +924,7 @@ __global__ void __launch_bounds__(kThreads)
             S->rmax32 = sqrtf(tot[1]);
             S->rmin32 = S->rmax32;
             S->need_update = 0;
+            S->xmax_bits = 0u;
         }
     }
 }
@@ -906,7 +937,10 @@ __global__ void __launch_bounds__(kThreads)
 // accumulator that stays in L2; half the matrix bytes for 1 + (upper blocks)
 // reductions per row.  The summation order of a row's contributions is that
 // of the reductions, so FP32 inner results vary in their last bits from run
-// to run (the FP64 residual and the stop test are computed as always).
+// to run (the FP64 residual and the stop test are computed as always).  This
+// form serves the mixed CG, whose iteration count does not follow those bits
+// (1841-1842 iterations on the 3.09M-DOF system); the mixed BiCGSTAB, whose
+// count does, uses the reproducible fixed-point form below.
 __device__ __forceinline__ void red_add_v4(float *a, float x, float y, float z)
 {
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(0.f)
@@ -1023,41 +1057,127 @@ __global__ void __launch_bounds__(kThreads, 5)
     }
 }
 
-// y = y4 (3 per block row), y4 = 0 for the next product, and the dot products
-// the full-storage SpMV kernels fuse, with their scalar updates:
-//   mode 0 (CG):        <a, y>          -> alpha = rho / <p, Ap>
-//   mode 1 (BiCGSTAB):  <a, y>          -> c2 = <r0, y>, alpha = c1 / c2
-//   mode 2 (BiCGSTAB):  <a, y>, <y, y>  -> c3 = <e, v> / <v, v>
-__global__ void __launch_bounds__(kThreads)
-    k_sym_finish(int64_t nb, float *__restrict__ y4, float *__restrict__ y, const float *__restrict__ a, int mode,
-                 KState *S, double *pd, float *pf, unsigned *ticket)
+// Reproducible form of the symmetric product (the BiCGSTAB inner iterations,
+// whose iteration count follows every rounding difference).  Each row's own
+// stored blocks are summed in FP32 by the lane that owns the row, in slot
+// order, and stored to y; the scattered transposes are converted to 64-bit
+// fixed point and added with integer reductions, which give the same total in
+// any order.  The quantum is a power of two chosen per product from a bound on
+// every partial sum, |sum| <= (max row sum of |A|) * max|x| < 2^61 / scale,
+// so no accumulator overflows; x's maximum comes from the kernel that wrote
+// x (KState::xmax_bits).  Terms smaller than the quantum (2^-61 of the bound)
+// are rounded to it.  k_symfx_finish adds the two parts in a fixed order.
+// Measured on the 3.09M-DOF system: 0.113 ms per product against 0.105 ms for
+// the FP32 vector reductions (an ordered gather of the transposes through a
+// transposed index, also reproducible, took 0.14-0.26 ms: latency-bound).
+__device__ __forceinline__ void red_add_u64(unsigned long long *a, long long v)
+{
+    asm volatile("red.global.add.u64 [%0], %1;" ::"l"(a), "l"(v));
+}
+
+// Exponent k of the fixed-point scale 2^k for a product whose partial sums are
+// bounded by rowsum * max|x|: bound * 2^k < 2^61.
+__device__ __forceinline__ int symfx_exponent(float rowsum, unsigned xmax_bits)
+{
+    const float bound = rowsum * __uint_as_float(xmax_bits);
+    if (!(bound > 0.f)) return 126;
+    if (!isfinite(bound)) return -67;
+    return min(126, 61 - (ilogbf(bound) + 1));
+}
+
+// y = (own stored blocks) x; acc64[t nb + c] += fixed-point transposes (three
+// planes: a warp's reductions of one component cover consecutive words; the
+// three components of a row in one sector made the reductions twice as slow)
+__global__ void __launch_bounds__(kThreads, 5)
+    k_spmv_symfx(SellView<float> U, const float *__restrict__ x, float *__restrict__ y,
+                 unsigned long long *__restrict__ acc64, float rowsum, const KState *S)
 {
     if (S->done | S->need_update) return;
-    Comp32 acc[2] = {Comp32{0.f, 0.f}, Comp32{0.f, 0.f}};
-    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
-         row += (int64_t)gridDim.x * blockDim.x) {
-        float4 *q = reinterpret_cast<float4 *>(y4 + 4 * row);
-        const float4 v = *q;
-        *q = make_float4(0.f, 0.f, 0.f, 0.f);
-        const float yv[3] = {v.x, v.y, v.z};
+    const float scale = exp2f((float)symfx_exponent(rowsum, S->xmax_bits));
+    PFG_SLICE_LOOP(U)
+    {
+        const int64_t row = s * 32 + lane;
+        const bool live = row < U.nb;
+        float xi[3];
 #pragma unroll
-        for (int t = 0; t < 3; ++t) {
-            y[3 * row + t] = yv[t];
-            comp_add_prod(acc[0], a[3 * row + t], yv[t]);
-            if (mode == 2) comp_add_prod(acc[1], yv[t], yv[t]);
+        for (int t = 0; t < 3; ++t) xi[t] = live ? __ldg(x + 3 * row + t) : 0.f;
+        const int64_t b0 = U.sptr[s];
+        const int w = (int)(U.sptr[s + 1] - b0);
+        const int *cp = U.col + b0 * 32 + lane;
+        const float *vp = U.val + b0 * 32 * 9 + lane;
+        float acc[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int k = 0; k < w; ++k) {
+            const int c = ld_stream(cp + (int64_t)k * 32);
+            float a[9];
+#pragma unroll
+            for (int e = 0; e < 9; ++e) a[e] = ld_stream(vp + ((int64_t)k * 9 + e) * 32);
+            float xj[3];
+#pragma unroll
+            for (int t = 0; t < 3; ++t) xj[t] = __ldg(x + 3 * (int64_t)c + t);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) acc[r] += fmaf(a[3 * r], xj[0], fmaf(a[3 * r + 1], xj[1], a[3 * r + 2] * xj[2]));
+            if (live && c != row) {
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    const float tv = fmaf(a[t], xi[0], fmaf(a[3 + t], xi[1], a[6 + t] * xi[2]));
+                    red_add_u64(acc64 + (int64_t)t * U.nb + c, __float2ll_rn(tv * scale));
+                }
+            }
+        }
+        if (live)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) y[3 * row + t] = acc[t];
+    }
+}
+
+// y += acc64 / scale (acc64 = 0 for the next product), then the dot products
+// and scalar updates of the BiCGSTAB products:
+//   mode 1:  <a, y>          -> c2 = <r0, y>, alpha = c1 / c2
+//   mode 2:  <a, y>, <y, y>  -> c3 = <e, v> / <v, v>
+// and xmax_bits = 0 for the next vector's maximum.  A thread per scalar entry
+// with four entries in flight (a thread per block row with its three entries
+// in turn was latency-bound: 88 us against 19 us at 3.09M DOF).
+__global__ void __launch_bounds__(kThreads)
+    k_symfx_finish(int64_t nb, float *__restrict__ y, unsigned long long *__restrict__ acc64,
+                   const float *__restrict__ a, float rowsum, int mode, KState *S, double *pd, float *pf,
+                   unsigned *ticket)
+{
+    if (S->done | S->need_update) return;
+    const float inv = exp2f((float)-symfx_exponent(rowsum, S->xmax_bits));
+    Comp32 acc[2] = {Comp32{0.f, 0.f}, Comp32{0.f, 0.f}};
+    const int64_t n = 3 * nb;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+        long long qv[4];
+        float yv[4], av[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            if (i < n) {
+                const int64_t row = i / 3;
+                qv[u] = (long long)acc64[(i - 3 * row) * nb + row];
+                yv[u] = y[i];
+                av[u] = a[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * stride;
+            if (i < n) {
+                const int64_t row = i / 3;
+                acc64[(i - 3 * row) * nb + row] = 0ull;
+                const float v = yv[u] + (float)qv[u] * inv;
+                y[i] = v;
+                comp_add_prod(acc[0], av[u], v);
+                if (mode == 2) comp_add_prod(acc[1], v, v);
+            }
         }
     }
     float tot[2];
     if (grid_total<2>(acc, pd, pf, ticket, tot)) {
-        if (mode == 0) {
-            const double pq = (double)tot[0];
-            if (!(pq > 0.0) || !finite_d(pq)) {
-                S->status = PFG_E_BREAKDOWN;
-                S->done = 1;
-            } else {
-                S->alpha32 = (float)(S->rho32 / tot[0]);
-            }
-        } else if (mode == 1) {
+        S->xmax_bits = 0u;  // every CTA read it at its start
+        if (mode == 1) {
             const double c2 = (double)tot[0];
             if (c2 == 0.0 || !finite_d(c2)) {
                 bicg_breakdown(S, false);
@@ -1329,8 +1449,8 @@ uint64_t Krylov::graph_key(int kind, const DevMatrix &A, const void *x, const KC
                     u(pA32_.p), u(pB32_.p), u(q32_.p), u(yA32_.p), u(yB32_.p), u(e32_.p), u(v32_.p), u(x32_.p),
                     u(dinv32_.p), u(ph_.p), u(eh_.p), u(ph32_.p), u(eh32_.p), u(partials_.p), u(partials32_.p), u(ticket_.p), u(state_.p),
                     (uint64_t)cfg.precond, (uint64_t)cfg.stop_rule, (uint64_t)cfg.graph_chunk, (uint64_t)cfg.itrmax,
-                    (uint64_t)cfg.fuse, (uint64_t)cfg.storage, u(y4_.p), u(A.sptr_u.p), u(A.scol_u.p),
-                    u(A.s32_u.p), d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta),
+                    (uint64_t)cfg.fuse, (uint64_t)cfg.storage, u(y4_.p), u(fx_.p), u(A.sptr_u.p), u(A.scol_u.p),
+                    u(A.s32_u.p), d((double)A.sym_rowsum), d(cfg.relative_er), d(cfg.er0), d(cfg.reliable_delta),
                     ilu_ ? ilu_->generation() : 0, u(ilu_ ? ilu_->lu() : nullptr)});
 }
 
@@ -1459,27 +1579,29 @@ static int cg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *
 }
 
 // One chunk of FP32 BiCGSTAB iterations with the symmetric matrix (the
-// separate-pass structure of bicg_chunk, each product through y4 + finish).
-static int bicg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *x, float *r, float *r0, float *p,
-                          float *y, float *e, float *v, float *ph, float *eh, float *y4, const float *dinv, int pc,
-                          KState *S, double *pd, float *pf, unsigned *tk, double er0, double tol, double delta,
-                          int itrmax, cudaStream_t st)
+// separate-pass structure of bicg_chunk): each product is the reproducible
+// fixed-point form (k_spmv_symfx + k_symfx_finish), and the direction and e
+// passes record the maximum of the vector the next product reads.
+static int bicg_chunk_sym(const SellView<float> &U, float rowsum, int chunk, int64_t nb, float *x, float *r,
+                          float *r0, float *p, float *y, float *e, float *v, float *ph, float *eh,
+                          unsigned long long *fx, const float *dinv, int pc, KState *S, double *pd, float *pf,
+                          unsigned *tk, double er0, double tol, double delta, int itrmax, cudaStream_t st)
 {
     const int64_t nvec = (nb * 3 + 31) / 32;
     float *phat = pc != PFG_PC_NONE ? ph : p;
     float *ehat = pc != PFG_PC_NONE ? eh : e;
     const int gd = resident_grid(k_bicg_dir<3, float>, (nb + 31) / 32);
     const int ge = resident_grid(k_bicg_e<3, float>, (nb + 31) / 32);
-    const int gs = resident_grid(k_spmv_sym, U.ns);
-    const int gf = resident_grid(k_sym_finish, (nb + 31) / 32);
+    const int gs = resident_grid(k_spmv_symfx, U.ns);
+    const int gf = resident_grid(k_symfx_finish, (3 * nb + 127) / 128);
     const int g3 = resident_grid(k_bicg_update<3, float>, nvec);
     for (int it = 0; it < chunk; ++it) {
-        k_bicg_dir<3, float><<<gd, kThreads, 0, st>>>(nb, r, p, y, ph, dinv, pc, S);
-        k_spmv_sym<<<gs, kThreads, 0, st>>>(U, phat, y4, S);
-        k_sym_finish<<<gf, kThreads, 0, st>>>(nb, y4, y, r0, 1, S, pd, pf, tk);
-        k_bicg_e<3, float><<<ge, kThreads, 0, st>>>(nb, r, y, e, eh, dinv, pc, S);
-        k_spmv_sym<<<gs, kThreads, 0, st>>>(U, ehat, y4, S);
-        k_sym_finish<<<gf, kThreads, 0, st>>>(nb, y4, v, e, 2, S, pd, pf, tk);
+        k_bicg_dir<3, float><<<gd, kThreads, 0, st>>>(nb, r, p, y, ph, dinv, pc, S, true);
+        k_spmv_symfx<<<gs, kThreads, 0, st>>>(U, phat, y, fx, rowsum, S);
+        k_symfx_finish<<<gf, kThreads, 0, st>>>(nb, y, fx, r0, rowsum, 1, S, pd, pf, tk);
+        k_bicg_e<3, float><<<ge, kThreads, 0, st>>>(nb, r, y, e, eh, dinv, pc, S, true);
+        k_spmv_symfx<<<gs, kThreads, 0, st>>>(U, ehat, v, fx, rowsum, S);
+        k_symfx_finish<<<gf, kThreads, 0, st>>>(nb, v, fx, e, rowsum, 2, S, pd, pf, tk);
         k_bicg_update<3, float><<<g3, kThreads, 0, st>>>(nb, x, r, r0, phat, phat, e, ehat, v, S, pd, pf, tk,
                                                          PFG_STOP_TRUE_RELATIVE, er0, tol, delta, itrmax);
     }
@@ -1735,10 +1857,16 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
     const int gv = grid_for(n, 256, sm_count() * 8);
     const bool sym = cfg.storage == PFG_STORAGE_SYMMETRIC;
     if (sym) {
-        // upper half (checked symmetric) and its zeroed 4-per-row accumulator
+        // upper half (checked symmetric) and its zeroed accumulator: 4 floats
+        // per row (CG) or three fixed-point planes (BiCGSTAB)
         build_sell_upper(A, st);
-        y4_.ensure((size_t)A.nb * 4);
-        PFG_CUDA(cudaMemsetAsync(y4_.p, 0, (size_t)A.nb * 4 * sizeof(float), st));
+        if (cg) {
+            y4_.ensure((size_t)A.nb * 4);
+            PFG_CUDA(cudaMemsetAsync(y4_.p, 0, (size_t)A.nb * 4 * sizeof(float), st));
+        } else {
+            fx_.ensure((size_t)A.nb * 3);
+            PFG_CUDA(cudaMemsetAsync(fx_.p, 0, (size_t)A.nb * 3 * sizeof(unsigned long long), st));
+        }
     }
     const uint64_t key = graph_key(cg ? 3 : 4, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
@@ -1753,10 +1881,10 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
                                   cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
                                   cfg.reliable_delta, cfg.itrmax, st);
             else if (sym)
-                nk = bicg_chunk_sym(sell_upper(A), ch, A.nb, x32_.p, r32_.p, r032_.p, pA32_.p, yA32_.p, e32_.p,
-                                    v32_.p, ph32_.p, eh32_.p, y4_.p, dinv32_.p, cfg.precond, state_.p, partials_.p,
-                                    partials32_.p, ticket_.p, cfg.er0, cfg.relative_er, cfg.reliable_delta,
-                                    cfg.itrmax, st);
+                nk = bicg_chunk_sym(sell_upper(A), A.sym_rowsum, ch, A.nb, x32_.p, r32_.p, r032_.p, pA32_.p,
+                                    yA32_.p, e32_.p, v32_.p, ph32_.p, eh32_.p, fx_.p, dinv32_.p, cfg.precond,
+                                    state_.p, partials_.p, partials32_.p, ticket_.p, cfg.er0, cfg.relative_er,
+                                    cfg.reliable_delta, cfg.itrmax, st);
             else if (cg)
                 nk = A.bs == 3 ? cg_chunk<3, float>(A.sell<float>(), fz, ch, A.nb, x32_.p, r32_.p, z32_.p, pA32_.p,
                                                     pB32_.p, q32_.p, dinv32_.p, cfg.precond, state_.p, partials_.p,
@@ -1958,7 +2086,7 @@ __global__ void k_fill(double *a, int64_t n, double v)
 
 void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
 {
-    PFG_CHECK(kernel >= 0 && kernel <= 9 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel >= 0 && kernel <= 10 && reps > 0, PFG_E_ARG, "bad profile request");
     if (kernel == 9) {
         // one D^-1 L^-1 sweep of the held ILU(0) factor (factored in
         // ascending column order if none is held)
@@ -1996,6 +2124,10 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
         y4_.ensure((size_t)A.nb * 4);
         PFG_CUDA(cudaMemsetAsync(y4_.p, 0, (size_t)A.nb * 4 * sizeof(float), st));
     }
+    if (kernel == 10) {
+        fx_.ensure((size_t)A.nb * 3);
+        PFG_CUDA(cudaMemsetAsync(fx_.p, 0, (size_t)A.nb * 3 * sizeof(unsigned long long), st));
+    }
     const int gv = grid_for(n, 256, sm_count() * 8);
     const int gb = row_grid(A.nb);
     DevBuf<double> x64, y64;
@@ -2003,6 +2135,7 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
     KState hs;
     memset(&hs, 0, sizeof(hs));
     hs.rho32 = 1.0f;
+    hs.xmax_bits = 0x3f800000u;  // max |x| = 1 (x is filled with ones)
     hs.beta32 = 0.5f;
     if (!state_.p) state_.alloc(1);
     if (!ticket_.p) {
@@ -2058,6 +2191,10 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
         case 8:
             k_cg_spmv_sym<<<resident_grid(k_cg_spmv_sym, A.ns_u), kThreads, 0, st>>>(
                 sell_upper(A), x32.p, y4_.p, state_.p, partials_.p, partials32_.p, ticket_.p);
+            break;
+        case 10:  // (its finish pass, which adds and clears the transposes, is not part of the launch)
+            k_spmv_symfx<<<resident_grid(k_spmv_symfx, A.ns_u), kThreads, 0, st>>>(sell_upper(A), x32.p, y32.p,
+                                                                                  fx_.p, A.sym_rowsum, state_.p);
             break;
         case 3:
             if (A.bs == 3) k_spmv<3, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);

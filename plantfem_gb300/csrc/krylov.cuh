@@ -29,6 +29,7 @@ struct KState {
     int replacements;      // mixed: number of FP64 residual replacements
     int breakdowns;        // mixed BiCGSTAB: FP32 breakdowns since the last completed iteration
     int poisoned;          // mixed: an FP32 update produced a non-finite value; drop x32
+    unsigned xmax_bits;    // max |v| (float bits) of the vector the next fixed-point symmetric product reads
 };
 
 struct KConfig {
@@ -80,6 +81,7 @@ struct DevMatrix {
     DevBuf<int> scol_u;
     DevBuf<float> s32_u;
     bool sell_u_pattern = false, s32_u_valid = false;
+    float sym_rowsum = 0.f;  // max over scalar rows of sum |a_ij| (FP32), set with s32_u
 
     // bumped whenever rp/col change: keys factors derived from the pattern
     uint64_t pattern_gen = 0;
@@ -180,7 +182,8 @@ class Krylov {
     // FP64 work vectors
     DevBuf<double> r_, r0_, z_, pA_, pB_, q_, yA_, yB_, e_, v_, dinv_, ph_, eh_;
     DevBuf<double> xb_;  // mixed: x before the fold of an FP32 correction
-    DevBuf<float> y4_;   // symmetric storage: 4-per-row product accumulator
+    DevBuf<float> y4_;   // symmetric storage: 4-per-row product accumulator (CG)
+    DevBuf<unsigned long long> fx_;  // symmetric storage: fixed-point transposes, 3 planes of nb (BiCGSTAB)
     // FP32 work vectors
     DevBuf<float> r32_, r032_, z32_, pA32_, pB32_, q32_, yA32_, yB32_, e32_, v32_, x32_, dinv32_, ph32_, eh32_;
     DevBuf<double> partials_;

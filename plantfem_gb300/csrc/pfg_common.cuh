@@ -108,8 +108,25 @@ struct DevBuf {
     T *get() const { return p; }
 };
 
-inline int grid_for(int64_t work, int per_block, int cap = 152 * 16)
+// Streaming multiprocessors of the current device (cached per device).
+inline int sm_count_device()
 {
+    static int cache[64] = {0};
+    int dev = 0;
+    PFG_CUDA(cudaGetDevice(&dev));
+    PFG_CHECK(dev >= 0 && dev < 64, PFG_E_UNSUPPORTED, "device ordinal above 63");
+    if (cache[dev] == 0) {
+        int v = 0;
+        PFG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+        cache[dev] = v > 0 ? v : 1;
+    }
+    return cache[dev];
+}
+
+// Blocks for `work` items, at most `cap` (default: 16 per SM of the device).
+inline int grid_for(int64_t work, int per_block, int cap = 0)
+{
+    if (cap <= 0) cap = sm_count_device() * 16;
     int64_t g = (work + per_block - 1) / per_block;
     if (g < 1) g = 1;
     if (g > cap) g = cap;

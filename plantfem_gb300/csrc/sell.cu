@@ -71,17 +71,17 @@ __global__ void __launch_bounds__(32 * kTileWarps)
     }
 }
 
-static int tile_grid(int64_t ns) { return (int)std::min<int64_t>((ns + kTileWarps - 1) / kTileWarps, 152 * 32); }
+static int tile_grid(int64_t ns) { return (int)std::min<int64_t>((ns + kTileWarps - 1) / kTileWarps, sm_count_device() * 32); }
 
 void build_sell(DevMatrix &A, bool want64, bool want32, cudaStream_t st)
 {
     PFG_CHECK(A.nb > 0, PFG_E_STATE, "empty matrix");
-    const int g = grid_for(A.nb, 256, 152 * 16);
+    const int g = grid_for(A.nb, 256, sm_count_device() * 16);
     if (!A.sell_pattern) {
         A.ns = (A.nb + 31) / 32;
         DevBuf<int64_t> width((size_t)A.ns + 1);
         PFG_CUDA(cudaMemsetAsync(width.p, 0, (A.ns + 1) * sizeof(int64_t), st));
-        k_sell_widths<<<grid_for(A.ns, 256, 152 * 16), 256, 0, st>>>(A.nb, A.ns, A.rp.p, width.p);
+        k_sell_widths<<<grid_for(A.ns, 256, sm_count_device() * 16), 256, 0, st>>>(A.nb, A.ns, A.rp.p, width.p);
         PFG_CUDA(cudaGetLastError());
         A.sptr.resize((size_t)A.ns + 1);
         const int64_t slots = exclusive_scan(width.p, A.sptr.p, A.ns + 1, st);
@@ -252,21 +252,49 @@ __global__ void k_sym_check(int64_t nb, const int64_t *__restrict__ rp, const in
     }
 }
 
+// max over scalar rows of sum_j |a_ij| (as FP32 bits), a warp per block row:
+// the bound the fixed-point symmetric product sizes its quantum from.
+__global__ void k_rowsum_max(int64_t nb, const int64_t *__restrict__ rp, const double *__restrict__ v64,
+                             unsigned *__restrict__ out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    float best = 0.f;
+    for (int64_t i = w0; i < nb; i += nw) {
+        const int64_t r0 = rp[i];
+        const int n = (int)(rp[i + 1] - r0);
+        float sum[3] = {0.f, 0.f, 0.f};
+        for (int k = lane; k < n; k += 32)
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) sum[r] += fabsf((float)v64[r0 * 9 + (int64_t)(3 * r + c) * n + k]);
+#pragma unroll
+        for (int r = 0; r < 3; ++r) best = fmaxf(best, warp_sum(sum[r]));
+    }
+    if (lane == 0) atomicMax(out, __float_as_uint(best));
+}
+
 void build_sell_upper(DevMatrix &A, cudaStream_t st)
 {
     PFG_CHECK(A.nb > 0, PFG_E_STATE, "empty matrix");
     PFG_CHECK(A.bs == 3, PFG_E_UNSUPPORTED, "symmetric storage is built for 3x3-block matrices");
     if (A.sell_u_pattern && A.s32_u_valid) return;
-    const int g = grid_for(A.nb, 256, 152 * 16);
+    const int g = grid_for(A.nb, 256, sm_count_device() * 16);
     // the values (pattern included) changed: check the symmetry once
     {
-        DevBuf<unsigned long long> bad(1);
-        PFG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(unsigned long long), st));
+        DevBuf<unsigned long long> bad(2);  // [0] asymmetric blocks, [1] low word: row-sum bound bits
+        PFG_CUDA(cudaMemsetAsync(bad.p, 0, 2 * sizeof(unsigned long long), st));
         k_sym_check<<<g, 256, 0, st>>>(A.nb, A.rp.p, A.col.p, A.v64.p, bad.p);
+        k_rowsum_max<<<g, 256, 0, st>>>(A.nb, A.rp.p, A.v64.p, reinterpret_cast<unsigned *>(bad.p + 1));
         PFG_CUDA(cudaGetLastError());
-        unsigned long long nbad = 0;
-        PFG_CUDA(cudaMemcpyAsync(&nbad, bad.p, sizeof nbad, cudaMemcpyDeviceToHost, st));
+        unsigned long long hb[2] = {0, 0};
+        PFG_CUDA(cudaMemcpyAsync(hb, bad.p, sizeof hb, cudaMemcpyDeviceToHost, st));
         PFG_CUDA(cudaStreamSynchronize(st));
+        const unsigned long long nbad = hb[0];
+        const unsigned rs_bits = (unsigned)(hb[1] & 0xffffffffull);  // little-endian low word
+        memcpy(&A.sym_rowsum, &rs_bits, sizeof rs_bits);
         PFG_CHECK(nbad == 0, PFG_E_ARG,
                   "symmetric storage needs a symmetric matrix: " + std::to_string(nbad) +
                       " blocks differ from their transposes");
@@ -275,7 +303,7 @@ void build_sell_upper(DevMatrix &A, cudaStream_t st)
         A.ns_u = (A.nb + 31) / 32;
         DevBuf<int64_t> width((size_t)A.ns_u + 1);
         PFG_CUDA(cudaMemsetAsync(width.p, 0, (A.ns_u + 1) * sizeof(int64_t), st));
-        k_sellu_widths<<<grid_for(A.ns_u, 256, 152 * 16), 256, 0, st>>>(A.nb, A.ns_u, A.rp.p, A.col.p, width.p);
+        k_sellu_widths<<<grid_for(A.ns_u, 256, sm_count_device() * 16), 256, 0, st>>>(A.nb, A.ns_u, A.rp.p, A.col.p, width.p);
         PFG_CUDA(cudaGetLastError());
         A.sptr_u.resize((size_t)A.ns_u + 1);
         const int64_t slots = exclusive_scan(width.p, A.sptr_u.p, A.ns_u + 1, st);

@@ -4,7 +4,9 @@ The mixed inner iterations may read only the upper 3x3 blocks of a symmetric
 matrix, applying each strictly-upper block also transposed.  Checked here:
 the solves agree with the FP64 oracle (CPU Jacobi-CG to 1e-13) to 1e-8 and
 with the full-storage mixed solve; the product itself equals the full FP32
-product to FP32 rounding; an unsymmetric matrix is refused with PFG_E_ARG.
+product to FP32 rounding; the mixed BiCGSTAB from the upper half (fixed-point
+transposes) is bitwise reproducible; an unsymmetric matrix is refused with
+PFG_E_ARG.
 """
 import ctypes as C
 
@@ -89,6 +91,43 @@ def test_symmetric_product_profiles(cuda):
         got[kid] = by.value
         assert ms.value > 0.0
     assert got[7] == got[8] and 0.45 * got[1] < got[7] < 0.65 * got[1]
+
+
+@pytest.mark.parametrize("pc", ["BlockJacobi", None])
+def test_symmetric_bicgstab_is_bitwise_reproducible(cuda, pc):
+    """Mixed BiCGSTAB from the upper half: the transposes are summed in 64-bit
+    fixed point, so repeated solves (same solver, then a fresh one) give the
+    same iterations and the same bits, and agree with the oracle to 1e-8."""
+    p, xo = _system(12, seed=5)
+    runs = []
+    s = None
+    for fresh in (True, False, True):
+        s = _solver(p) if fresh else s
+        s.relative_er = 1e-12
+        x = s.solve(algorithm="BiCGSTAB", preconditioning=pc, precision="mixed", stop_rule="true_relative",
+                    storage="symmetric")
+        assert s.last_info["status"] == 0 and s.last_info["fallback"] == 0, s.last_info
+        assert _rel(x, xo) <= 1e-8
+        runs.append((x, s.last_info["iterations"], s.last_info["replacements"]))
+    for x, it, rep in runs[1:]:
+        assert (it, rep) == runs[0][1:]
+        np.testing.assert_array_equal(x, runs[0][0])
+
+
+def test_fixed_point_product_profiles(cuda):
+    """Kernel 10 (the BiCGSTAB product from the upper half) runs and reports the
+    upper half's bytes, like kernel 7."""
+    p, _ = _system(8)
+    s = _solver(p)
+    s.eliminate()
+    lib = N.load()
+    got = {}
+    for kid in (7, 10):
+        ms, by = C.c_double(), C.c_double()
+        N.check(lib.pfg_profile_kernel(s.handle, kid, 3, C.byref(ms), C.byref(by)))
+        got[kid] = by.value
+        assert ms.value > 0.0
+    assert got[7] == got[10]
 
 
 def test_unsymmetric_matrix_is_refused(cuda):
