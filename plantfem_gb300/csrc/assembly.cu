@@ -248,16 +248,31 @@ __device__ __forceinline__ double shape_N(int a, int gp)
 // along the first column (MathClass.f90:1460-1476), inverse_rank_2
 // (MathClass.f90:1584-1593), and G[a][p] = JPsy(p, a) with
 // JPsy = transpose(matmul(transpose(dNdgzi), Jin)) (FEMDomainClass.f90:12289).
-__device__ __forceinline__ double gp_geometry(const double (*xe)[3], int gp, double (*G)[3])
+__device__ __forceinline__ double gp_geometry_dn(const double (*xe)[3], const double (*dN)[8], double (*G)[3]);
+
+// dN/dxi at Gauss point gp (3 x 8), the values gp_geometry computes.
+__device__ __forceinline__ void gp_dshape(int gp, double (*dN)[8])
 {
     const double g0 = c_sgx[gp] * PFG_GP, g1 = c_sgy[gp] * PFG_GP, g2 = c_sgz[gp] * PFG_GP;
-    double dN[3][8];
 #pragma unroll
     for (int a = 0; a < 8; ++a) {
         dN[0][a] = 0.125 * c_sgx[a] * (1.0 + c_sgy[a] * g1) * (1.0 + c_sgz[a] * g2);
         dN[1][a] = 0.125 * c_sgy[a] * (1.0 + c_sgx[a] * g0) * (1.0 + c_sgz[a] * g2);
         dN[2][a] = 0.125 * c_sgz[a] * (1.0 + c_sgx[a] * g0) * (1.0 + c_sgy[a] * g1);
     }
+}
+
+__device__ __forceinline__ double gp_geometry(const double (*xe)[3], int gp, double (*G)[3])
+{
+    double dN[3][8];
+    gp_dshape(gp, dN);
+    return gp_geometry_dn(xe, dN, G);
+}
+
+// gp_geometry with dN/dxi given (the element kernel keeps the eight Gauss
+// points' tables in shared memory: they are the same for every element).
+__device__ __forceinline__ double gp_geometry_dn(const double (*xe)[3], const double (*dN)[8], double (*G)[3])
+{
     double J[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -308,140 +323,211 @@ __device__ __forceinline__ int64_t find_slot(const int64_t *__restrict__ rp, con
     return -1;
 }
 
-// Block (a, b) of the element matrix.  Stiffness: B^T D B detJ summed over the
-// Gauss points (FEMDomainClass.f90:11504-11511), written through the Lame form
-// K_ab[i][j] = sum_gp detJ (lambda g_a,i g_b,j + mu g_a,j g_b,i + mu (g_a.g_b) d_ij),
-// which equals the product with B of :12283-12305 and D of :11626-11637.
-// Mass: rho sum_gp N_a N_b detJ I3 (FEMDomainClass.f90:10934-10936).
-struct ElemSmem {
-    double x[8][3];
-    double G[8][8][3];  // [gp][node][dim]
-    double W[8];        // detJ per Gauss point
-    int node[8];
-};
+// Element matrices, four threads per element.  Stiffness: B^T D B detJ summed
+// over the Gauss points (FEMDomainClass.f90:11504-11511).  With the Lame
+// constants of the element and P_ab = sum_gp detJ g_a g_b^T (g_a the
+// gradient of N_a through the reference's J^-T form), the 3x3 block is
+// K_ab = lambda P_ab + mu P_ab^T + mu tr(P_ab) I, the product with B of
+// :12283-12305 and D of :11626-11637 written out.  Mass: rho sum_gp N_a N_b
+// detJ I3 (FEMDomainClass.f90:10934-10936); row-lumped (:10940-10948): the
+// row sums on the diagonal blocks.  Only the 36 blocks b >= a are computed
+// (K and M are symmetric); each is added at (a, b) and, transposed, at (b, a).
+// Thread s of an element takes block rows s and 7 - s (nine blocks each).
+// Node coordinates, gradients and detJ of the eight Gauss points live in
+// shared memory (the four threads compute two Gauss points each); the slot
+// of every block in its CRS row comes from the element's slot map (built
+// once per pattern), so the scatter does no search.  FP64-bound: about 4.5k
+// DFMA per stiffness element.
+constexpr int kEPC = 16;  // elements per CTA
 
-__device__ __forceinline__ void stiff_block(const ElemSmem &S, int a, int b, double lam, double mu, double (&K)[3][3])
-{
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) K[i][j] = 0.0;
-#pragma unroll
-    for (int gp = 0; gp < 8; ++gp) {
-        const double w = S.W[gp];
-        const double ga0 = S.G[gp][a][0], ga1 = S.G[gp][a][1], ga2 = S.G[gp][a][2];
-        const double gb0 = S.G[gp][b][0], gb1 = S.G[gp][b][1], gb2 = S.G[gp][b][2];
-        const double la[3] = {w * lam * ga0, w * lam * ga1, w * lam * ga2};
-        const double ma[3] = {w * mu * ga0, w * mu * ga1, w * mu * ga2};
-        const double gb[3] = {gb0, gb1, gb2};
-        const double dd = ma[0] * gb0 + ma[1] * gb1 + ma[2] * gb2;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) K[i][j] += la[i] * gb[j] + ma[j] * gb[i] + (i == j ? dd : 0.0);
-    }
-}
-
-constexpr int kEPB = 2;  // elements per CTA, 64 threads each (one per node pair)
-
-// mode 0: scatter into K (coloured, no atomics); mode 1: write 24x24 to out.
-__global__ void __launch_bounds__(64 * kEPB)
+template <int GPU, int MINB>
+__global__ void __launch_bounds__(4 * kEPC, MINB)
     k_element_matrix(int64_t n_el, const int *__restrict__ elems, const double *__restrict__ xyz, int64_t nn,
                      const int *__restrict__ conn, int64_t ne, int kind, const double *__restrict__ p0,
                      const double *__restrict__ p1, int bcast, const int64_t *__restrict__ rp,
-                     const int *__restrict__ col, double *__restrict__ val, int mode, double *__restrict__ out,
+                     const uint16_t *__restrict__ slots, double *__restrict__ val, int mode, double *__restrict__ out,
                      int *err)
 {
-    __shared__ ElemSmem sm[kEPB];
-    const int g = threadIdx.x >> 6, t = threadIdx.x & 63;
-    for (int64_t base = (int64_t)blockIdx.x * kEPB; base < n_el; base += (int64_t)gridDim.x * kEPB) {
-        const int64_t li = base + g;
+    __shared__ double sX[kEPC][8][3];
+    __shared__ double sH[kEPC][8][8][3];  // [element][gp][node][dim]: sqrt|detJ| g (G itself where detJ <= 0)
+    __shared__ double sW[kEPC][8];
+    __shared__ double sDN[8][3][8];       // dN/dxi per Gauss point
+    __shared__ int sNode[kEPC][8];
+    __shared__ int sPos[kEPC];            // every detJ of the element > 0
+    const int q = threadIdx.x >> 2, sub = threadIdx.x & 3;
+    for (int gp = threadIdx.x; gp < 8; gp += blockDim.x) gp_dshape(gp, sDN[gp]);
+    __syncthreads();
+    for (int64_t base = (int64_t)blockIdx.x * kEPC; base < n_el; base += (int64_t)gridDim.x * kEPC) {
+        const int64_t li = base + q;
         const bool valid = li < n_el;
         const int e = valid ? (elems ? elems[li] : (int)li) : 0;
-        ElemSmem &S = sm[g];
-        if (valid && t < 8) {
-            const int v = conn[(int64_t)t * ne + e];
-            S.node[t] = v;
-            S.x[t][0] = xyz[v];
-            S.x[t][1] = xyz[nn + v];
-            S.x[t][2] = xyz[2 * nn + v];
-        }
-        __syncthreads();
-        if (valid && t < 8) {
-            const double det = gp_geometry(S.x, t, S.G[t]);
-            S.W[t] = det;
-            if (det == 0.0) *err = 1;
-        }
-        __syncthreads();
-        if (valid) {
-            const int a = t >> 3, b = t & 7;
-            double K[3][3];
-            bool active;
-            if (kind == 0) {
-                double lam, mu;
-                lame(bcast ? p0[0] : p0[e], bcast ? p1[0] : p1[e], lam, mu);
-                active = (mode == 1) || b >= a;
-                if (active) stiff_block(S, a, b, lam, mu, K);
-            } else {
-                const double rho = bcast ? p0[0] : p0[e];
-                double m = 0.0;
-                if (kind == 1) {
-                    active = (mode == 1) || b >= a;
+        if (valid)
 #pragma unroll
-                    for (int gp = 0; gp < 8; ++gp) m += shape_N(a, gp) * shape_N(b, gp) * S.W[gp];
-                    m *= rho;
-                } else {  // row-lumped (FEMDomainClass.f90:10940-10948): only diagonal blocks
-                    active = (a == b);
-                    if (active)
-                        for (int bb = 0; bb < 8; ++bb) {
-                            double mb = 0.0;
-#pragma unroll
-                            for (int gp = 0; gp < 8; ++gp) mb += shape_N(a, gp) * shape_N(bb, gp) * S.W[gp];
-                            m += rho * mb;
-                        }
-                    if (mode == 1) active = true, m = (a == b) ? m : 0.0;
-                }
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) K[i][j] = (i == j) ? m : 0.0;
+            for (int h = 0; h < 2; ++h) {
+                const int v = sub + 4 * h;
+                const int node = conn[(int64_t)v * ne + e];
+                sNode[q][v] = node;
+                sX[q][v][0] = xyz[node];
+                sX[q][v][1] = xyz[nn + node];
+                sX[q][v][2] = xyz[2 * nn + node];
             }
-            if (active) {
-                if (mode == 1) {
-                    double *o = out + (int64_t)e * 576;
+        __syncwarp();
+        bool pos = true;
+        if (valid)
 #pragma unroll
-                    for (int i = 0; i < 3; ++i)
+            for (int h = 0; h < 2; ++h) {
+                const int gp = sub + 4 * h;
+                const double det = gp_geometry_dn(sX[q], sDN[gp], sH[q][gp]);
+                sW[q][gp] = det;
+                if (det == 0.0) *err = 1;
+                pos = pos && det > 0.0;
+            }
+        {  // the element's four lanes (a quad of the warp) agree on whether every detJ > 0
+            int pv = pos ? 1 : 0;
+            pv &= __shfl_xor_sync(0xffffffffu, pv, 1);
+            pv &= __shfl_xor_sync(0xffffffffu, pv, 2);
+            pos = pv != 0;
+        }
+        __syncwarp();
+        if (valid && kind == 0) {
+            // P_ab = sum_gp detJ g_a g_b^T = sum_gp h_a h_b^T with h = sqrt(detJ) g when
+            // every detJ > 0; otherwise G stays and each term takes its detJ
+            if (sub == 0) sPos[q] = pos ? 1 : 0;
 #pragma unroll
-                        for (int j = 0; j < 3; ++j) o[(3 * b + j) * 24 + 3 * a + i] = K[i][j];
-                } else {
-                    const int ra = S.node[a], rb = S.node[b];
-                    int nblk;
-                    const int64_t k = find_slot(rp, col, ra, rb, nblk);
-                    if (k < 0) {
-                        *err = 2;
+            for (int h = 0; h < 2; ++h) {
+                const int gp = sub + 4 * h;
+                if (pos) {
+                    const double r = sqrt(sW[q][gp]);
+#pragma unroll
+                    for (int v = 0; v < 8; ++v)
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) sH[q][gp][v][d] *= r;
+                }
+            }
+        }
+        __syncwarp();
+        if (valid) {
+            double lam = 0.0, mu = 0.0, rho = 0.0;
+            if (kind == 0)
+                lame(bcast ? p0[0] : p0[e], bcast ? p1[0] : p1[e], lam, mu);
+            else
+                rho = bcast ? p0[0] : p0[e];
+            const uint16_t *sl = slots ? slots + (int64_t)e * 64 : nullptr;
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+                const int a = h == 0 ? sub : 7 - sub;
+#pragma unroll 1
+                for (int b = a; b < 8; ++b) {
+                    double K[3][3];
+                    if (kind == 0) {
+                        double P[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}};
+                        if (sPos[q]) {
+#pragma unroll GPU
+                            for (int gp = 0; gp < 8; ++gp) {
+                                const double ha[3] = {sH[q][gp][a][0], sH[q][gp][a][1], sH[q][gp][a][2]};
+                                const double hb[3] = {sH[q][gp][b][0], sH[q][gp][b][1], sH[q][gp][b][2]};
+#pragma unroll
+                                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                                    for (int j = 0; j < 3; ++j) P[i][j] = fma(ha[i], hb[j], P[i][j]);
+                            }
+                        } else {
+                            for (int gp = 0; gp < 8; ++gp) {
+                                const double w = sW[q][gp];
+                                const double wa[3] = {w * sH[q][gp][a][0], w * sH[q][gp][a][1], w * sH[q][gp][a][2]};
+                                const double gb[3] = {sH[q][gp][b][0], sH[q][gp][b][1], sH[q][gp][b][2]};
+#pragma unroll
+                                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                                    for (int j = 0; j < 3; ++j) P[i][j] = fma(wa[i], gb[j], P[i][j]);
+                            }
+                        }
+                        const double mt = mu * (P[0][0] + P[1][1] + P[2][2]);
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j)
+                                K[i][j] = fma(lam, P[i][j], mu * P[j][i]) + (i == j ? mt : 0.0);
                     } else {
-                        double *v = val + rp[ra] * 9 + k;
+                        double m = 0.0;
+                        if (kind == 1) {
+#pragma unroll
+                            for (int gp = 0; gp < 8; ++gp) m += shape_N(a, gp) * shape_N(b, gp) * sW[q][gp];
+                            m *= rho;
+                        } else if (a == b) {
+                            for (int bb = 0; bb < 8; ++bb) {
+                                double mb = 0.0;
+#pragma unroll
+                                for (int gp = 0; gp < 8; ++gp) mb += shape_N(a, gp) * shape_N(bb, gp) * sW[q][gp];
+                                m += rho * mb;
+                            }
+                        }
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) K[i][j] = (i == j) ? m : 0.0;
+                        if (kind == 2 && a != b && mode == 0) continue;  // lumped: diagonal blocks only
+                    }
+                    if (mode == 1) {
+                        double *o = out + (int64_t)e * 576;
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int j = 0; j < 3; ++j) {
+                                o[(3 * b + j) * 24 + 3 * a + i] = K[i][j];
+                                if (a != b) o[(3 * a + i) * 24 + 3 * b + j] = K[i][j];
+                            }
+                        continue;
+                    }
+                    {
+                        const int ra = sNode[q][a];
+                        const int64_t r0 = rp[ra];
+                        const int nblk = (int)(rp[ra + 1] - r0);
+                        double *v = val + r0 * 9 + sl[a * 8 + b];
 #pragma unroll
                         for (int i = 0; i < 3; ++i)
 #pragma unroll
                             for (int j = 0; j < 3; ++j) v[(int64_t)(3 * i + j) * nblk] += K[i][j];
                     }
                     if (a != b) {
-                        const int64_t k2 = find_slot(rp, col, rb, ra, nblk);
-                        if (k2 < 0) {
-                            *err = 2;
-                        } else {
-                            double *v = val + rp[rb] * 9 + k2;
+                        const int rb = sNode[q][b];
+                        const int64_t r0 = rp[rb];
+                        const int nblk = (int)(rp[rb + 1] - r0);
+                        double *v = val + r0 * 9 + sl[b * 8 + a];
 #pragma unroll
-                            for (int i = 0; i < 3; ++i)
+                        for (int i = 0; i < 3; ++i)
 #pragma unroll
-                                for (int j = 0; j < 3; ++j) v[(int64_t)(3 * j + i) * nblk] += K[i][j];
-                        }
+                            for (int j = 0; j < 3; ++j) v[(int64_t)(3 * j + i) * nblk] += K[i][j];
                     }
                 }
             }
         }
-        __syncthreads();
+        __syncwarp();
+    }
+}
+
+// Slot map of the coloured assembly: slots[e * 64 + a * 8 + b] = position of
+// block column node(b) in block row node(a).  A thread per (element, a).
+// err = 2: a block has no slot (not the mesh's pattern); 3: a row longer than
+// 65,535 blocks.
+__global__ void k_slot_map(int64_t ne, const int *__restrict__ conn, const int64_t *__restrict__ rp,
+                           const int *__restrict__ col, uint16_t *__restrict__ slots, int *err)
+{
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ne * 8;
+         t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = t >> 3;
+        const int a = (int)(t & 7);
+        const int row = conn[(int64_t)a * ne + e];
+        const int64_t r0 = rp[row];
+        const int n = (int)(rp[row + 1] - r0);
+        if (n > 65535) *err = 3;
+        for (int b = 0; b < 8; ++b) {
+            const int c = conn[(int64_t)b * ne + e];
+            int k = 0;
+            while (k < n && col[r0 + k] != c) ++k;
+            if (k == n) *err = 2;
+            slots[e * 64 + a * 8 + b] = (uint16_t)(k < n ? k : 0);
+        }
     }
 }
 
@@ -454,20 +540,61 @@ static void check_err(DevBuf<int> &err, cudaStream_t st)
     PFG_CHECK(h != 2, PFG_E_MISSING_SLOT, "no CRS slot for an element block (fill-in request)");
 }
 
+static void ensure_slot_map(const DevMesh &m, const DevMatrix &K, cudaStream_t st)
+{
+    if (m.slots_gen == K.pattern_gen && m.slots.p) return;
+    m.slots.resize((size_t)m.ne * 64);
+    DevBuf<int> err(1);
+    PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
+    k_slot_map<<<grid_for(m.ne * 8, 256), 256, 0, st>>>(m.ne, m.conn.p, K.rp.p, K.col.p, m.slots.p, err.p);
+    PFG_CUDA(cudaGetLastError());
+    int h = 0;
+    PFG_CUDA(cudaMemcpyAsync(&h, err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PFG_CUDA(cudaStreamSynchronize(st));
+    PFG_CHECK(h != 2, PFG_E_MISSING_SLOT, "no CRS slot for an element block (fill-in request)");
+    PFG_CHECK(h != 3, PFG_E_UNSUPPORTED, "a CRS block row longer than 65,535 blocks");
+    m.slots_gen = K.pattern_gen;
+}
+
+template <typename Kern>
+static int element_grid(Kern kern, int64_t n)
+{
+    int per_sm = 0;
+    PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 4 * kEPC, 0));
+    if (per_sm <= 0) per_sm = 1;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + kEPC - 1) / kEPC, (int64_t)per_sm * sm_count_device()));
+}
+
+// The element kernel's configuration: Gauss-point loop unrolled 4x, at least
+// 6 CTAs per SM (168 registers).  Measured at 100^3 (1M elements, 8 colour
+// launches): 22.1 ms against 23.2 ms fully unrolled (252 registers) and
+// 27.1 ms at 128 registers (spills).
+using ElementKernel = void (*)(int64_t, const int *, const double *, int64_t, const int *, int64_t, int,
+                               const double *, const double *, int, const int64_t *, const uint16_t *, double *, int,
+                               double *, int *);
+static const ElementKernel kElementKernel = k_element_matrix<4, 6>;
+
+template <typename... Args>
+static void launch_element_matrix(int64_t n, cudaStream_t st, Args... args)
+{
+    kElementKernel<<<element_grid(kElementKernel, n), 4 * kEPC, 0, st>>>(n, args...);
+}
+
 void assemble_elements(const DevMesh &m, DevMatrix &K, int kind, const double *p0, const double *p1, bool broadcast,
                        cudaStream_t st)
 {
     PFG_CHECK(K.bs == 3 && K.nb == m.nn, PFG_E_STATE, "pattern not built for this mesh (call setCRS(DOF=3))");
     PFG_CHECK(!m.color_ptr.empty(), PFG_E_STATE, "mesh not coloured");
+    ensure_slot_map(m, K, st);
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
     for (size_t c = 0; c + 1 < m.color_ptr.size(); ++c) {
         const int64_t n = m.color_ptr[c + 1] - m.color_ptr[c];
         if (n == 0) continue;
-        const int grid = (int)std::min<int64_t>((n + kEPB - 1) / kEPB, sm_count_device() * 16);
-        k_element_matrix<<<grid, 64 * kEPB, 0, st>>>(n, m.color_elems.p + m.color_ptr[c], m.xyz.p, m.nn, m.conn.p,
-                                                      m.ne, kind, p0, p1, broadcast ? 1 : 0, K.rp.p, K.col.p,
-                                                      K.v64.p, 0, nullptr, err.p);
+        launch_element_matrix(n, st, (const int *)(m.color_elems.p + m.color_ptr[c]), (const double *)m.xyz.p,
+                              m.nn, (const int *)m.conn.p, m.ne, kind, p0, p1, broadcast ? 1 : 0,
+                              (const int64_t *)K.rp.p, (const uint16_t *)m.slots.p, K.v64.p, 0, (double *)nullptr,
+                              err.p);
         PFG_CUDA(cudaGetLastError());
     }
     K.values_changed();
@@ -479,9 +606,9 @@ void element_stiffness(const DevMesh &m, const double *E, const double *nu, bool
 {
     DevBuf<int> err(1);
     PFG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), st));
-    const int grid = (int)std::min<int64_t>((m.ne + kEPB - 1) / kEPB, sm_count_device() * 16);
-    k_element_matrix<<<grid, 64 * kEPB, 0, st>>>(m.ne, nullptr, m.xyz.p, m.nn, m.conn.p, m.ne, 0, E, nu,
-                                                  broadcast ? 1 : 0, nullptr, nullptr, nullptr, 1, out, err.p);
+    launch_element_matrix(m.ne, st, (const int *)nullptr, (const double *)m.xyz.p, m.nn, (const int *)m.conn.p,
+                          m.ne, 0, E, nu, broadcast ? 1 : 0, (const int64_t *)nullptr, (const uint16_t *)nullptr,
+                          (double *)nullptr, 1, out, err.p);
     PFG_CUDA(cudaGetLastError());
     check_err(err, st);
 }

@@ -15,6 +15,10 @@ struct DevMesh {
     // elements grouped by colour: no two elements of one colour share a node
     DevBuf<int> color_elems;
     std::vector<int64_t> color_ptr;
+    // per element, the slot of each of its 64 blocks in the CRS rows of the
+    // pattern with generation slots_gen (built by the first assembly)
+    mutable DevBuf<uint16_t> slots;
+    mutable uint64_t slots_gen = 0;
 };
 
 // Build the node-graph pattern in the reference's first-appearance order

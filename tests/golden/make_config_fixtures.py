@@ -1,0 +1,253 @@
+"""Oracle fixtures for the five benchmark configurations at their stated sizes.
+
+Run from the repository root (CPU only; the large stages take minutes to an
+hour on 8 cores):
+
+    python tests/golden/make_config_fixtures.py [stage ...]
+
+Stages (default: all, in this order): ``patterns``, ``cfg1``, ``cfg2``,
+``cfg2_bicgstab``, ``cfg4``, ``cfg5``, ``cfg3``, ``manifest`` (re-hashes every
+fixture, for stages run in separate processes).  Each stage writes one
+compressed ``configs/<stage>.npz`` and records its SHA-256 in
+``configs/MANIFEST.json``.  The GPU tests compare the CUDA path with these
+files, so the oracle itself never runs at full size inside a test.
+
+What each fixture holds (the FP64 oracle is ``oracle.pcg``: Jacobi CG to the
+true relative residual 1e-12 on the oracle-assembled, Dirichlet-eliminated
+scalar CRS, standing in for the reference's own FEMSolver_ solve at tol 1e-12):
+
+* ``patterns``: SHA-256 of ``ZeroMatrix_as_CRS`` (``orc_zero_matrix``)
+  row_ptr (int64) and col_idx (int32) bytes for Cube3D 20^3, 60^3, 64^3, 100^3.
+* ``cfg1``: 20^3 cube, E = 1e4: the oracle solution in full, and
+  ``bicgstab_CRS_2`` with the reference stop rule (relative_er = er0 = 1e-10):
+  its solution and iteration count.
+* ``cfg2``: 100^3 lognormal (seed 20261203): the oracle solution's norm, max,
+  and a seeded sample of 50,000 entries (seed 2026), the fixed DOF ids.
+* ``cfg2_bicgstab``: the iteration count of the oracle's ``bicgstab_CRS_2``
+  (reference stop rule, 1e-10) on the cfg2 system, the count the CPU
+  reference arm is scaled by.
+* ``cfg4``: 64^3, parameter field E (seed 2), target field (seed 1): the
+  oracle gradient dL/dE = -lambda_e^T (dK_e/dE_e) u_e of
+  L = 0.5 |u - u_t|^2 at the 32 elements drawn by seed 3, a seeded sample of
+  4,096 more, the gradient's largest magnitude and the loss.
+* ``cfg5``: the 512 slabs of seed 5: each slab's solution norm and 64 seeded
+  entries (seed 55), by a direct sparse solve (SuperLU) of the oracle system
+  with three steps of iterative refinement on the oracle's residual: the
+  clamped thin slabs are too ill conditioned for Jacobi CG to reach 1e-12
+  (a plain direct solve leaves relative residuals up to ~1e-9).
+* ``cfg3``: 60^3 cantilever, the lowest 20 eigenvalues of the fix_eig-reduced
+  pencil by the oracle's ``LOBPCG_CRS`` restatement (block 24, TOL 1e-8).
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+import time
+
+import numpy as np
+import scipy.sparse.linalg as spla
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "configs")
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from oracle import lobpcg as OL  # noqa: E402
+from plantfem_gb300 import problems  # noqa: E402  (host-side mesh and load builders, no GPU)
+
+TOL = 1e-12
+SAMPLE_SEED_CFG2 = 2026
+SAMPLE_SEED_CFG4 = 2027
+SAMPLE_SEED_CFG5 = 55
+
+
+def _log(msg):
+    print(f"[{time.strftime('%H:%M:%S')}] {msg}", flush=True)
+
+
+def _save(name, **arrays):
+    os.makedirs(OUT, exist_ok=True)
+    path = os.path.join(OUT, name + ".npz")
+    np.savez_compressed(path, **arrays)
+    mpath = os.path.join(OUT, "MANIFEST.json")
+    man = json.load(open(mpath)) if os.path.exists(mpath) else {
+        "generator": "tests/golden/make_config_fixtures.py (CPU oracle)", "files": {}}
+    man["files"][name + ".npz"] = hashlib.sha256(open(path, "rb").read()).hexdigest()
+    with open(mpath, "w") as f:
+        json.dump(man, f, indent=1, sort_keys=True)
+    _log(f"wrote {path}")
+
+
+def eliminated_system(p, E=None):
+    """Oracle pattern, assembly and Dirichlet elimination of a problem dict."""
+    dom = p["domain"]
+    rp, ci = O.zero_matrix(dom.nn(), dom.elemnod, 3)
+    val = O.assemble(dom.nodcoord, dom.elemnod, rp, ci, "stiffness", E=p["E"] if E is None else E, nu=p["nu"])
+    b = p["rhs"].copy()
+    fixed = np.zeros(3 * dom.nn(), np.uint8)
+    fixed[p["fix_ids"] - 1] = 1
+    O.apply_fix(rp, ci, val, b, fixed, np.zeros(3 * dom.nn()))
+    return rp, ci, val, b, fixed
+
+
+def stage_patterns():
+    out = {}
+    for n in (20, 60, 64, 100):
+        xyz, en = O.cube3d(n, n, n)
+        t = time.time()
+        rp, ci = O.zero_matrix(xyz.shape[0], en, 3)
+        out[f"rp_sha256_{n}"] = np.array(hashlib.sha256(rp.astype("<i8").tobytes()).hexdigest())
+        out[f"ci_sha256_{n}"] = np.array(hashlib.sha256(ci.astype("<i4").tobytes()).hexdigest())
+        out[f"nnz_{n}"] = np.int64(ci.shape[0])
+        _log(f"pattern {n}^3: nnz {ci.shape[0]} ({time.time() - t:.1f} s)")
+        del rp, ci
+    _save("patterns", **out)
+
+
+def stage_cfg1():
+    p = problems.cube(20)
+    rp, ci, val, b, fixed = eliminated_system(p)
+    x, rc, it, rr = O.pcg(rp, ci, val, b, tol=TOL)
+    assert rc == 0, rr
+    xb, rcb, itb = O.bicgstab_crs2(rp, ci, val, b, er0=1e-10, relative_er=1e-10)
+    assert rcb == 0
+    _log(f"cfg1: pcg {it} iterations, relres {rr:.2e}; bicgstab_CRS_2 {itb} iterations")
+    _save("cfg1", x=x, pcg_iterations=np.int64(it), pcg_relres=np.float64(rr), x_bicgstab=xb,
+          bicgstab_iterations=np.int64(itb), fixed=fixed)
+
+
+def stage_cfg2():
+    p = problems.lognormal(100)
+    t = time.time()
+    rp, ci, val, b, fixed = eliminated_system(p)
+    _log(f"cfg2: assembled in {time.time() - t:.1f} s")
+    t = time.time()
+    x, rc, it, rr = O.pcg(rp, ci, val, b, tol=TOL)
+    assert rc == 0, rr
+    _log(f"cfg2: pcg {it} iterations, relres {rr:.2e} ({time.time() - t:.0f} s)")
+    idx = np.sort(np.random.default_rng(SAMPLE_SEED_CFG2).choice(x.shape[0], 50000, replace=False))
+    _save("cfg2", idx=idx.astype(np.int64), x_sample=x[idx], x_norm=np.float64(np.linalg.norm(x)),
+          x_max=np.float64(np.abs(x).max()), pcg_iterations=np.int64(it), pcg_relres=np.float64(rr),
+          fixed_ids=np.nonzero(fixed)[0].astype(np.int64), seed=np.int64(p["seed"]))
+
+
+def stage_cfg2_bicgstab():
+    p = problems.lognormal(100)
+    rp, ci, val, b, _ = eliminated_system(p)
+    t = time.time()
+    x, rc, it = O.bicgstab_crs2(rp, ci, val, b, er0=1e-10, relative_er=1e-10)
+    el = time.time() - t
+    r = b - O.spmv(rp, ci, val, x)
+    relres = np.linalg.norm(r) / np.linalg.norm(b)
+    _log(f"cfg2 bicgstab_CRS_2: rc {rc}, {it} iterations, true relres {relres:.2e} ({el:.0f} s)")
+    _save("cfg2_bicgstab", iterations=np.int64(it), rc=np.int64(rc), true_relres=np.float64(relres),
+          seconds=np.float64(el), threads=np.int64(O.num_threads()))
+
+
+def stage_cfg4():
+    n, n_fd = 64, 32
+    p = problems.lognormal(n, seed=2)
+    dom = p["domain"]
+    ne = dom.ne()
+    E_t = problems.lognormal_E(ne, seed=1)
+    rp, ci, val_t, b, fixed = eliminated_system(p, E=E_t)
+    u_t, rc, it, _ = O.pcg(rp, ci, val_t, b, tol=TOL)
+    assert rc == 0
+    del val_t
+    _log(f"cfg4: target solve {it} iterations")
+    _, _, val, b, _ = eliminated_system(p)
+    u, rc, it, _ = O.pcg(rp, ci, val, b, tol=TOL)
+    assert rc == 0
+    _log(f"cfg4: forward solve {it} iterations")
+    g = u - u_t
+    g[fixed == 1] = 0.0
+    lam, rc, it, _ = O.pcg(rp, ci, val, g, tol=TOL)
+    assert rc == 0
+    _log(f"cfg4: adjoint solve {it} iterations")
+    Kh = O.element_stiffness_all(dom.nodcoord, dom.elemnod, 1.0, p["nu"])
+    en = dom.elemnod - 1
+    dofs = (3 * en[:, :, None] + np.arange(3)[None, None, :]).reshape(-1, 24)
+    grad = -np.einsum("ei,eij,ej->e", lam[dofs], Kh, u[dofs])
+    fd = np.random.default_rng(3).choice(ne, size=n_fd, replace=False)
+    extra = np.sort(np.random.default_rng(SAMPLE_SEED_CFG4).choice(ne, size=4096, replace=False))
+    _save("cfg4", fd_elements=fd.astype(np.int64), grad_fd=grad[fd], sample_elements=extra.astype(np.int64),
+          grad_sample=grad[extra], grad_max=np.float64(np.abs(grad).max()),
+          loss=np.float64(0.5 * np.dot(u - u_t, u - u_t)), u_norm=np.float64(np.linalg.norm(u)))
+
+
+def stage_cfg5(count=512, seed=5):
+    nx, ny, nz, rng = problems.slab_sizes(count, seed=seed)
+    Es = np.exp(rng.normal(np.log(1e4), 0.5, size=count))
+    srng = np.random.default_rng(SAMPLE_SEED_CFG5)
+    norms, samples, idxs, dofs, relress = [], [], [], [], []
+    worst = 0.0
+    t = time.time()
+    for k in range(count):
+        p = problems.slab(int(nx[k]), int(ny[k]), int(nz[k]), Es[k])
+        rp, ci, val, b, _ = eliminated_system(p)
+        lu = spla.splu(O.crs_to_scipy(rp, ci, val).tocsc())
+        x = lu.solve(b)
+        for _ in range(3):  # iterative refinement with the oracle's residual
+            dx = lu.solve(b - O.spmv(rp, ci, val, x))
+            x = x + dx
+        # the computed residual's floor is eps |A| |x| (up to ~2e-9 here);
+        # the last refinement step bounds the solution's own error
+        relres = np.linalg.norm(b - O.spmv(rp, ci, val, x)) / np.linalg.norm(b)
+        step = np.linalg.norm(dx) / np.linalg.norm(x)
+        assert relres <= 1e-8 and step <= 1e-9, (k, relres, step)
+        worst = max(worst, relres)
+        relress.append(relres)
+        idx = np.sort(srng.choice(x.shape[0], 64, replace=False))
+        norms.append(np.linalg.norm(x))
+        samples.append(x[idx])
+        idxs.append(idx)
+        dofs.append(x.shape[0])
+    _log(f"cfg5: {count} slabs, {sum(dofs)} DOF, worst direct-solve relres {worst:.1e} ({time.time() - t:.0f} s)")
+    _save("cfg5", x_norm=np.array(norms), idx=np.array(idxs, dtype=np.int64), x_sample=np.array(samples),
+          dof=np.array(dofs, dtype=np.int64), E=Es, nx=nx, ny=ny, nz=nz, direct_relres=np.array(relress))
+
+
+def stage_cfg3(n=60, nev=20, block=24, tol=1e-8):
+    p = problems.cantilever(n)
+    dom = p["domain"]
+    rp, ci = O.zero_matrix(dom.nn(), dom.elemnod, 3)
+    K = O.assemble(dom.nodcoord, dom.elemnod, rp, ci, "stiffness", E=p["E"], nu=p["nu"])
+    M = O.assemble(dom.nodcoord, dom.elemnod, rp, ci, "mass", rho=p["rho"])
+    rk, ck, vk = O.reduce_crs(rp, ci, K, p["fix_ids"])
+    rm, cm, vm = O.reduce_crs(rp, ci, M, p["fix_ids"])
+    del K, M, rp, ci
+    A = O.CrsOperator(rk, ck, vk)
+    B = O.CrsOperator(rm, cm, vm)
+    _log(f"cfg3: reduced pencil of {A.shape[0]} DOF")
+    t = time.time()
+    lam, X, it = OL.lobpcg_crs(A, B, block, max_itr=5000, tol=tol, seed=0, return_iters=True)
+    _log(f"cfg3: LOBPCG {it} iterations ({time.time() - t:.0f} s)")
+    # relative residuals of the wanted pairs, |K x - lambda M x| / |lambda M x|
+    AX, BX = A @ X[:, :nev], B @ X[:, :nev]
+    res = np.linalg.norm(AX - BX * lam[None, :nev], axis=0) / np.linalg.norm(BX * lam[None, :nev], axis=0)
+    _log(f"cfg3: lambda_1 {lam[0]:.10g}, lambda_{nev} {lam[nev - 1]:.10g}, max rel residual {res.max():.2e}")
+    _save("cfg3", eigenvalues=lam[:nev], block_eigenvalues=lam, rel_residuals=res, iterations=np.int64(it),
+          ndof_reduced=np.int64(A.shape[0]), tol=np.float64(tol))
+
+
+def stage_manifest():
+    """Re-hash every fixture into MANIFEST.json (after stages ran separately)."""
+    files = sorted(f for f in os.listdir(OUT) if f.endswith(".npz"))
+    man = {"generator": "tests/golden/make_config_fixtures.py (CPU oracle)",
+           "files": {f: hashlib.sha256(open(os.path.join(OUT, f), "rb").read()).hexdigest() for f in files}}
+    with open(os.path.join(OUT, "MANIFEST.json"), "w") as fh:
+        json.dump(man, fh, indent=1, sort_keys=True)
+    _log(f"manifest: {len(files)} files")
+
+
+STAGES = {"patterns": stage_patterns, "cfg1": stage_cfg1, "cfg2": stage_cfg2, "cfg2_bicgstab": stage_cfg2_bicgstab,
+          "cfg4": stage_cfg4, "cfg5": stage_cfg5, "cfg3": stage_cfg3, "manifest": stage_manifest}
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(STAGES)
+    for s in names:
+        _log(f"stage {s}")
+        STAGES[s]()
