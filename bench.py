@@ -326,6 +326,7 @@ def modal_lines(n=60, nev=20, block=24, tol=1e-8):
     s.assembleStiffness(p["E"], p["nu"])
     s.keepThisMatrixAs("A")
     s.fix_eig(p["fix_ids"])
+    s.use_LOBPCG = True
     s.LOBPCG_TOL = tol
     s.LOBPCG_MAX_ITR = 3000
     out = {"workload": f"cantilever{n}: {3 * p['domain'].nn()} DOF, {len(p['fix_ids'])} fixed, nev {nev}, "

@@ -265,6 +265,20 @@ void pfg_eig_opts_default(pfg_eig_opts *opts);
 int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *eigen_value, double *eigen_vectors,
             pfg_info *info);
 
+/* The dense branch of FEMSolver_%eig (use_LOBPCG = .false., the reference's
+ * default; FEMSolverClass.f90:1384-1541 with DSPGVD at :1470-1500): every
+ * eigenpair of A z = lambda B z for the matrices kept as "A" and "B", with the
+ * fix_eig DOFs removed (reduce_crs_matrix order), computed in FP64 on the GPU
+ * (Cholesky of B, C = L^-1 A L^-T, cyclic Jacobi, back substitution).
+ * num_eigen <= 0: all N pairs (N from pfg_eig_reduced_size), else the lowest
+ * min(num_eigen, N).  eigen_value ascending; eigen_vectors (may be NULL):
+ * ndof x count column-major, B-orthonormal, zero at the fixed DOFs.  At most
+ * 4096 unknowns (PFG_E_UNSUPPORTED above: the packed dense problem grows as
+ * N^2); B not positive definite: PFG_E_ARG.  info->iterations = Jacobi sweeps. */
+int pfg_eig_dense(pfg_solver *h, int32_t num_eigen, double *eigen_value, double *eigen_vectors, pfg_info *info);
+/* Size N of the fix_eig-reduced eigenproblem of the matrices kept as "A"/"B". */
+int pfg_eig_reduced_size(pfg_solver *h, int64_t *n);
+
 /* ------------------------------------------------ reference-signature plug-ins */
 /* crs_spmv_real64(val, row_ptr, col_idx, old_vector, new_vector, n, col_size)
  * (SparseClass-c.c:53-65, bound at SparseClass.f90:38-51): new_vector += A *

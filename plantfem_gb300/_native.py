@@ -123,6 +123,8 @@ SIGNATURES = {
     "pfg_load_matrix": (C.c_int, [_P, C.c_char_p]),
     "pfg_eig_opts_default": (None, [C.POINTER(EigOpts)]),
     "pfg_eig": (C.c_int, [_P, C.POINTER(EigOpts), _i32, _P, _P, C.POINTER(Info)]),
+    "pfg_eig_dense": (C.c_int, [_P, _i32, _P, _P, C.POINTER(Info)]),
+    "pfg_eig_reduced_size": (C.c_int, [_P, C.POINTER(_i64)]),
     "pfg_linear_solver_crs_noalloc": (C.c_int, [_P, _P, _P, _P, _P, _i64, C.POINTER(SolveOpts), C.POINTER(Info),
                                                 _P]),
     "pfg_eliminate": (C.c_int, [_P]),

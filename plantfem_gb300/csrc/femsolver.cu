@@ -7,6 +7,7 @@
 // copied in at set*/fix and out at solve/eig/getCRS, like the reference's
 // value-semantics setters.
 #include <algorithm>
+#include <numeric>
 #include <chrono>
 #include <cmath>
 #include <mutex>
@@ -748,6 +749,90 @@ int pfg_fix_eig(pfg_solver *h, int64_t n, const int32_t *ids)
         std::sort(h->fix_eig_ids.begin(), h->fix_eig_ids.end());
         h->fix_eig_ids.erase(std::unique(h->fix_eig_ids.begin(), h->fix_eig_ids.end()), h->fix_eig_ids.end());
     });
+}
+
+int pfg_eig_reduced_size(pfg_solver *h, int64_t *n)
+{
+    return guard([&] {
+        need(h && n, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        DevMatrix *A = find_slot(h, "A");
+        need(A, PFG_E_STATE, "no matrix kept as \"A\" (keepThisMatrixAs)");
+        int64_t nf = 0;
+        for (int id : h->fix_eig_ids) nf += (id >= 1 && id <= A->ndof());
+        *n = A->ndof() - nf;
+    });
+}
+
+int pfg_eig_dense(pfg_solver *h, int32_t num_eigen, double *eigen_value, double *eigen_vectors, pfg_info *info)
+{
+    int status = PFG_OK;
+    const int rc = guard([&] {
+        need(h && eigen_value, PFG_E_ARG, "NULL argument");
+        std::lock_guard<std::mutex> lk(h->mu);
+        DevMatrix *A = find_slot(h, "A"), *B = find_slot(h, "B");
+        need(A && B, PFG_E_STATE, "eig needs matrices kept as \"A\" and \"B\" (keepThisMatrixAs)");
+        need(A->nb == B->nb && A->bs == B->bs, PFG_E_ARG, "A and B differ in size or block structure");
+        const auto t0 = std::chrono::steady_clock::now();
+        const int64_t n = A->ndof();
+        // reduce_crs_matrix order: the remaining DOFs keep their order
+        std::vector<int> map((size_t)n, 0);
+        for (int id : h->fix_eig_ids)
+            if (id >= 1 && id <= n) map[(size_t)id - 1] = -1;
+        std::vector<int64_t> old_of_new;
+        for (int64_t i = 0; i < n; ++i)
+            if (map[(size_t)i] == 0) {
+                map[(size_t)i] = (int)old_of_new.size();
+                old_of_new.push_back(i);
+            }
+        const int64_t N = (int64_t)old_of_new.size();
+        need(N >= 1, PFG_E_ARG, "every DOF is fixed (fix_eig)");
+        PFG_CHECK(N <= kDenseEigMax, PFG_E_UNSUPPORTED,
+                  "dense eig (use_LOBPCG = .false.): " + std::to_string(N) + " unknowns, at most " +
+                      std::to_string(kDenseEigMax) + " on this path; set use_LOBPCG for larger problems");
+        const int64_t num = num_eigen > 0 ? std::min<int64_t>(num_eigen, N) : N;
+        DevBuf<int> dmap((size_t)n);
+        PFG_CUDA(cudaMemcpyAsync(dmap.p, map.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, h->st));
+        DevBuf<double> dA((size_t)(N * N)), dB((size_t)(N * N)), dZ((size_t)(N * N));
+        PFG_CUDA(cudaMemsetAsync(dA.p, 0, dA.bytes(), h->st));
+        PFG_CUDA(cudaMemsetAsync(dB.p, 0, dB.bytes(), h->st));
+        k_dense_from_blocks<<<grid_for(A->nb, 128), 128, 0, h->st>>>(A->nb, A->bs, A->rp.p, A->col.p, A->v64.p,
+                                                                    dmap.p, (int)N, dA.p);
+        k_dense_from_blocks<<<grid_for(B->nb, 128), 128, 0, h->st>>>(B->nb, B->bs, B->rp.p, B->col.p, B->v64.p,
+                                                                    dmap.p, (int)N, dB.p);
+        PFG_CUDA(cudaGetLastError());
+        std::vector<double> w((size_t)N);
+        int sweeps = 0;
+        dense_generalized_eig((int)N, dA.p, dB.p, w.data(), dZ.p, &sweeps, h->st);
+        std::vector<int> order((size_t)N);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return w[(size_t)a] < w[(size_t)b]; });
+        for (int64_t k = 0; k < num; ++k) eigen_value[k] = w[(size_t)order[(size_t)k]];
+        if (eigen_vectors) {
+            // scatter back to every DOF, zero at the fixed ones (eigFEMSolver :1498-1539)
+            std::vector<double> Z((size_t)(N * N));
+            PFG_CUDA(cudaMemcpyAsync(Z.data(), dZ.p, dZ.bytes(), cudaMemcpyDeviceToHost, h->st));
+            PFG_CUDA(cudaStreamSynchronize(h->st));
+            std::fill(eigen_vectors, eigen_vectors + n * num, 0.0);
+            for (int64_t k = 0; k < num; ++k) {
+                const int c = order[(size_t)k];
+                double *x = eigen_vectors + k * n;
+                for (int64_t r = 0; r < N; ++r) x[old_of_new[(size_t)r]] = Z[(size_t)(r * N + c)];
+            }
+        }
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (info) {
+            info->status = status;
+            info->iterations = sweeps;
+            info->replacements = 0;
+            info->kernel_launches = 0;
+            info->rel_residual = 0.0;
+            info->iter_residual = 0.0;
+            info->solve_ms = ms;
+            info->fallback = 0;
+        }
+    });
+    return rc != PFG_OK ? rc : status;
 }
 
 int pfg_eig(pfg_solver *h, const pfg_eig_opts *opts, int32_t num_eigen, double *eigen_value, double *eigen_vectors,

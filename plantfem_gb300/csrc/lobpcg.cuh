@@ -57,4 +57,15 @@ EigResult lobpcg_solve(DevMatrix &K, DevMatrix &M, const uint8_t *fixed, const E
 // written to lam and C (m x k column-major).
 int small_generalized_eig(int m, const double *A, const double *B, int k, double rank_tol, double *lam, double *C);
 
+// The dense branch of FEMSolver_%eig (dense_eig.cu): every eigenpair of
+// A z = lambda B z for dense row-major N x N device matrices (both destroyed;
+// B symmetric positive definite, else PFG_E_ARG).  w (host, N): eigenvalues
+// in the order of Z's columns (unsorted); Z (device, N x N row-major): the
+// B-orthonormal eigenvectors as columns.  *sweeps: Jacobi sweeps done.
+constexpr int kDenseEigMax = 4096;
+int dense_generalized_eig(int N, double *A, double *B, double *w, double *Z, int *sweeps, cudaStream_t st);
+__global__ void k_dense_from_blocks(int64_t nb, int bs, const int64_t *__restrict__ rp, const int *__restrict__ col,
+                                    const double *__restrict__ v, const int *__restrict__ map, int N,
+                                    double *__restrict__ D);
+
 }  // namespace pfg

@@ -318,10 +318,22 @@ class FEMSolver:
             eigen_vectors: bool = True, tol_fp32: float | None = None):
         """(eigen_value, eigen_vectors) = FEMSolver_%eig (FEMSolverClass.f90:1384-1541).
 
-        Always LOBPCG (LOBPCG_CRS, SparseClass.f90:2008-2239) on the matrices
-        kept as "A" and "B"; the reference's dense DSPGVD branch is an O(N^2)
-        CPU path.  Uses LOBPCG_NUM_MODE / LOBPCG_TOL / LOBPCG_MAX_ITR.
+        As the reference, on the matrices kept as "A" and "B" with the fix_eig
+        DOFs removed, and by ``use_LOBPCG``:
+
+        * ``use_LOBPCG = False`` (the reference's default): the dense branch
+          (DSPGVD, :1470-1500) -- every eigenpair (or the lowest
+          ``num_eigen``), on the GPU by pfg_eig_dense, at most 4096 unknowns;
+        * ``use_LOBPCG = True``: LOBPCG (LOBPCG_CRS, SparseClass.f90:2008-2239)
+          for ``num_eigen`` (default LOBPCG_NUM_MODE) pairs with LOBPCG_TOL /
+          LOBPCG_MAX_ITR; ``block_size``, ``precision`` ("mixed": FP32 phase
+          then FP64), ``preconditioning`` and ``stop_rule`` select its form.
+
+        eigen_vectors: ndof x count, zero at the fixed DOFs (None with
+        ``eigen_vectors=False``).
         """
+        if not self.use_LOBPCG:
+            return self._eig_dense(num_eigen, eigen_vectors)
         nev = int(num_eigen or self.LOBPCG_NUM_MODE)
         o = N.EigOpts()
         self._lib.pfg_eig_opts_default(C.byref(o))
@@ -342,6 +354,19 @@ class FEMSolver:
         info = N.Info()
         N.check(self._lib.pfg_eig(self._h, C.byref(o), nev, N.ptr(lam), None if X is None else N.ptr(X),
                                   C.byref(info)))
+        self.last_info = info.as_dict()
+        return lam, (None if X is None else X.T)
+
+    def _eig_dense(self, num_eigen, eigen_vectors=True):
+        nred = C.c_int64()
+        N.check(self._lib.pfg_eig_reduced_size(self._h, C.byref(nred)))
+        count = nred.value if not num_eigen or num_eigen <= 0 else min(int(num_eigen), nred.value)
+        lam = np.zeros(count)
+        n = self.ndof()
+        X = np.zeros((count, n)) if eigen_vectors else None
+        info = N.Info()
+        N.check(self._lib.pfg_eig_dense(self._h, int(num_eigen or 0), N.ptr(lam),
+                                        None if X is None else N.ptr(X), C.byref(info)))
         self.last_info = info.as_dict()
         return lam, (None if X is None else X.T)
 

@@ -1,4 +1,4 @@
-"""SeismicAnalysis: linear Newmark-beta time stepping with Rayleigh damping.
+"""SeismicAnalysis: modal analysis and linear Newmark-beta time stepping.
 
 Mirrors the fields and the step of plantFEM's ``SeismicAnalysis_``
 (SeismicAnalysisClass.f90: defaults :98-109, ``LinearReyleighNewmark``
@@ -62,6 +62,55 @@ class SeismicAnalysis:
         self.U, self.V, self.A, self.A_ext = (a for a, _ in self._pins)
         self._s = None
         return self
+
+    # the reference's constant in the frequency of modalAnalysis
+    # (SeismicAnalysisClass.f90:1805: freq = sqrt(|lambda|) / 2 / 3.141590)
+    _PI_MODAL = 3.141590
+
+    def modalAnalysis(self, femdomain: FEMDomain, YoungModulus, PoissonRatio, Density, fix_node_list_x=None,
+                      fix_node_list_y=None, fix_node_list_z=None, num_eigen: int | None = None,
+                      use_LOBPCG: bool = False, **eig_kw):
+        """SeismicAnalysis_%modalAnalysis (SeismicAnalysisClass.f90:1715-1834).
+
+        Assembles the consistent mass (kept as "B") and the stiffness (kept as
+        "A") with per-element Density / YoungModulus / PoissonRatio, removes
+        the listed nodes' x, y and z DOFs (1-based node ids -> DOF
+        (id - 1) * 3 + d, fix_eig), solves the generalized eigenproblem --
+        by default every pair with the dense branch, as the reference's
+        ``eig()`` call does; ``use_LOBPCG`` (with ``num_eigen`` and
+        ``eig_kw`` for FEMSolver.eig) for large meshes -- and sets
+        ``frequency = sqrt(|lambda|) / 2 / 3.141590`` and ``ModeVectors``, each
+        mode with a non-zero frequency scaled to unit 2-norm.
+        Returns (frequency, ModeVectors).
+        """
+        ne = femdomain.ne()
+        self.YoungModulus = np.broadcast_to(np.asarray(YoungModulus, dtype=np.float64), (ne,)).copy()
+        self.PoissonRatio = np.broadcast_to(np.asarray(PoissonRatio, dtype=np.float64), (ne,)).copy()
+        self.Density = np.broadcast_to(np.asarray(Density, dtype=np.float64), (ne,)).copy()
+        self.femdomain = femdomain
+        s = FEMSolver()
+        s.setDomain(femdomain)
+        s.setCRS(3)
+        s.assembleMass(self.Density)
+        s.keepThisMatrixAs("B")
+        s.zeros()
+        s.assembleStiffness(self.YoungModulus, self.PoissonRatio)
+        s.keepThisMatrixAs("A")
+        for d, lst in enumerate((fix_node_list_x, fix_node_list_y, fix_node_list_z)):
+            if lst is not None and len(lst) > 0:
+                s.fix_eig((np.asarray(lst, dtype=np.int64) - 1) * 3 + d + 1)
+        s.use_LOBPCG = bool(use_LOBPCG)
+        lam, X = s.eig(num_eigen, **eig_kw)
+        freq = np.sqrt(np.abs(lam)) / 2.0 / self._PI_MODAL
+        for i in range(freq.shape[0]):
+            if freq[i] == 0.0:
+                continue
+            X[:, i] = X[:, i] / np.linalg.norm(X[:, i])
+        self.frequency = freq
+        self.ModeVectors = X
+        self.last_info = dict(s.last_info)
+        s.remove()
+        return freq, X
 
     def fixDisplacement(self, NodeList, direction: str, disp: float = 0.0):
         """Prescribed displacement of nodes (1-based ids) in x, y or z

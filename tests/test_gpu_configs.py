@@ -150,6 +150,7 @@ def test_config3_eigenvalues_vs_oracle(cuda, precision):
     s.assembleStiffness(p["E"], p["nu"])
     s.keepThisMatrixAs("A")
     s.fix_eig(p["fix_ids"])
+    s.use_LOBPCG = True
     s.LOBPCG_TOL = 1e-8
     s.LOBPCG_MAX_ITR = 3000
     lam, _ = s.eig(20, block_size=24, precision=precision, eigen_vectors=False)
