@@ -188,7 +188,10 @@ int pfg_eliminate(pfg_solver *h);
 /* getElementCauchyStress(displacement, E, v, option) (FEMDomainClass.f90:15249-15330,
  * StressMatrix :11912-12035): cell-averaged Cauchy stress of every element from the
  * node-interleaved displacement (3*nn, host).  option 0: full 3x3 tensors (out: ne*9,
- * row-major), 1: I1 = trace ("I1"), 2: mean stress trace/3 ("p") (out: ne).  E, v:
+ * row-major); otherwise one value per element (out: ne), the reference's options
+ * (:15310-15362): 1 I1 = trace, 2 p = trace/3, 3 I2 = (tr(S)^2 - tr(S S))/2,
+ * 4 I3 = det S, 5 / 6 / 7 the same three of the deviator S - tr(S)/3 I (J1, J2,
+ * J3), 10 + 3 (i-1) + (j-1) the component S(i, j) (the (i, j) form).  E, v:
  * n_prop = 1 or ne values. */
 int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop, const double *E, const double *v,
                        int32_t option, double *out);

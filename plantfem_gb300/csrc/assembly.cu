@@ -795,6 +795,63 @@ __global__ void k_stress(int64_t ne, const double *__restrict__ xyz, int64_t nn,
     }
 }
 
+// One number per element from its cell-averaged stress tensor S (row-major),
+// the options of getElementCauchyStress (FEMDomainClass.f90:15310-15362):
+// 1 I1 = tr S, 2 p = tr S / 3, 3 I2 = (tr(S)^2 - tr(S S)) / 2, 4 I3 = det S
+// (cofactors along the first column, det_mat of MathClass.f90:1460-1476),
+// 5-7 the same three of the deviator s = S - tr(S)/3 I (J1 = tr s, J2, J3),
+// 10 + 3 (i-1) + (j-1): the component S(i, j).  Other codes leave 0, as the
+// reference's select case does for an unknown option.
+__device__ __forceinline__ double det3_first_column(const double *a)
+{
+    return a[0] * (a[4] * a[8] - a[7] * a[5]) - a[3] * (a[1] * a[8] - a[7] * a[2]) +
+           a[6] * (a[1] * a[5] - a[4] * a[2]);
+}
+
+__global__ void k_stress_option(int64_t ne, const double *__restrict__ S, int option, double *__restrict__ out)
+{
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+        double a[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) a[k] = S[e * 9 + k];
+        double r = 0.0;
+        if (option >= 10 && option <= 18) {
+            r = a[option - 10];
+        } else if (option >= 1 && option <= 7) {
+            double tr = a[0] + a[4] + a[8];
+            if (option >= 5) {  // the deviator
+                const double m = tr / 3.0;
+                a[0] -= m;
+                a[4] -= m;
+                a[8] -= m;
+                tr = a[0] + a[4] + a[8];
+            }
+            const int inv = option >= 5 ? option - 4 : (option == 2 ? 0 : (option == 1 ? 1 : option - 1));
+            if (inv == 0) {
+                r = tr / 3.0;
+            } else if (inv == 1) {
+                r = tr;
+            } else if (inv == 2) {
+                double trss = 0.0;  // tr(S S)
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) trss += a[3 * i + k] * a[3 * k + i];
+                r = (tr * tr - trss) * 0.5;
+            } else {
+                r = det3_first_column(a);
+            }
+        }
+        out[e] = r;
+    }
+}
+
+void element_stress_option(int64_t ne, const double *S, int option, double *out, cudaStream_t st)
+{
+    k_stress_option<<<grid_for(ne, 256), 256, 0, st>>>(ne, S, option, out);
+    PFG_CUDA(cudaGetLastError());
+}
+
 void element_stress(const DevMesh &m, const double *disp, const double *E, const double *nu, bool broadcast,
                     double *out, cudaStream_t st)
 {

@@ -50,6 +50,10 @@ void element_stiffness(const DevMesh &m, const double *E, const double *nu, bool
 // Cell-averaged Cauchy stress (ne x 9, row-major 3x3) from a 3*nn displacement.
 void element_stress(const DevMesh &m, const double *disp, const double *E, const double *nu, bool broadcast,
                     double *out, cudaStream_t st);
+// One value per element from the stress tensors (ne x 9, device): the options
+// of getElementCauchyStress (1 I1, 2 p, 3 I2, 4 I3, 5 J1, 6 J2, 7 J3,
+// 10 + 3 (i-1) + (j-1) component (i, j)); out: ne values (device).
+void element_stress_option(int64_t ne, const double *S, int option, double *out, cudaStream_t st);
 // Adjoint sensitivity g_e = -lambda_e^T (dK_e/dE_e) u_e for every element.
 void adjoint_grad_E(const DevMesh &m, const double *u, const double *lam, const double *nu, bool broadcast,
                     double *grad, cudaStream_t st);

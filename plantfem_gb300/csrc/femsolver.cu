@@ -990,7 +990,8 @@ int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop
 {
     return guard([&] {
         need(h && displacement && E && v && out, PFG_E_ARG, "NULL argument");
-        need(option >= 0 && option <= 2, PFG_E_ARG, "option: 0 tensor, 1 I1, 2 mean stress");
+        need((option >= 0 && option <= 7) || (option >= 10 && option <= 18), PFG_E_ARG,
+             "option: 0 tensor, 1 I1, 2 p, 3 I2, 4 I3, 5 J1, 6 J2, 7 J3, 10 + 3 (i-1) + (j-1) component (i, j)");
         std::lock_guard<std::mutex> lk(h->mu);
         need(h->have_mesh, PFG_E_STATE, "stress before setDomain");
         const int64_t ne = h->mesh.ne, n = 3 * h->mesh.nn;
@@ -999,17 +1000,14 @@ int pfg_element_stress(pfg_solver *h, const double *displacement, int64_t n_prop
         upload_prop(h, n_prop, v, dnu, "v");
         PFG_CUDA(cudaMemcpyAsync(du.p, displacement, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
         element_stress(h->mesh, du.p, dE.p, dnu.p, n_prop == 1, S.p, h->st);
-        std::vector<double> hs((size_t)ne * 9);
-        PFG_CUDA(cudaMemcpyAsync(hs.data(), S.p, ne * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
-        PFG_CUDA(cudaStreamSynchronize(h->st));
         if (option == 0) {
-            memcpy(out, hs.data(), ne * 9 * sizeof(double));
+            PFG_CUDA(cudaMemcpyAsync(out, S.p, ne * 9 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
         } else {
-            for (int64_t e = 0; e < ne; ++e) {
-                const double tr = hs[e * 9] + hs[e * 9 + 4] + hs[e * 9 + 8];
-                out[e] = option == 1 ? tr : tr / 3.0;  // getElementCauchyStress options (FEMDomainClass.f90:15310-15314)
-            }
+            DevBuf<double> r((size_t)ne);
+            element_stress_option(ne, S.p, option, r.p, h->st);
+            PFG_CUDA(cudaMemcpyAsync(out, r.p, ne * sizeof(double), cudaMemcpyDeviceToHost, h->st));
         }
+        PFG_CUDA(cudaStreamSynchronize(h->st));
     });
 }
 

@@ -260,14 +260,45 @@ class FEMSolver:
         to the stored matrix and RHS now (solve() does it itself)."""
         N.check(self._lib.pfg_eliminate(self._h))
 
-    def getElementCauchyStress(self, displacement, E, v, option: str | None = None):
-        """getElementCauchyStress (FEMDomainClass.f90:15249): cell-averaged stress per
-        element; option None -> (ne, 3, 3) tensors, "I1" -> trace, "p" -> trace / 3."""
+    # option strings of getElementCauchyStress (FEMDomainClass.f90:15310-15362)
+    _STRESS_OPTIONS = {**{k: 2 for k in ("p", "P")},
+                       **{k: 1 for k in ("I", "I1", "i1", "trace", "tr", "TRACE", "TR")},
+                       **{k: 3 for k in ("II", "I2", "i2", "ii")},
+                       **{k: 4 for k in ("III", "I3", "i3", "iii")},
+                       **{k: 5 for k in ("J", "J1", "j1", "j")},
+                       **{k: 6 for k in ("JJ", "J2", "j2", "jj")},
+                       **{k: 7 for k in ("JJJ", "J3", "j3", "jjj")},
+                       **{f"{a}{i},{j}{b}": 10 + 3 * (i - 1) + (j - 1)
+                          for i, j in ((1, 1), (2, 2), (3, 3)) for a, b in (("", ""), ("(", ")"), ("_{", "}"))},
+                       **{f"{a}{p},{q}{b}": 10 + 3 * (i - 1) + (j - 1)
+                          for i, j in ((1, 2), (1, 3), (2, 3)) for p, q in ((i, j), (j, i))
+                          for a, b in (("", ""), ("(", ")"), ("_{", "}"))}}
+
+    def getElementCauchyStress(self, displacement, E, v, i: int | None = None, j: int | None = None,
+                               option: str | None = None):
+        """getElementCauchyStress (FEMDomainClass.f90:15249-15370): cell-averaged
+        Cauchy stress per element (StressMatrix, :11912-12035).
+
+        * ``i, j`` given (1-based): the component sigma(i, j) of every element;
+        * ``option``: one invariant or component per element -- "p", "I1" (and
+          "I", "trace", ...), "I2", "I3", "J1", "J2", "J3" (of the deviator, as
+          the reference computes them: J2 = (tr(s)^2 - tr(s s)) / 2), or
+          "1,1" ... "3,2" in any of the reference's spellings; an option the
+          reference does not know gives zeros, as its ``select case`` does;
+        * neither: the (ne, 3, 3) tensors.
+        """
         d = _f64(displacement)
         Ev = _f64(np.atleast_1d(E))
         vv = _f64(np.broadcast_to(np.atleast_1d(v), Ev.shape))
         ne = self.domain.ne()
-        opt = {None: 0, "I1": 1, "I": 1, "trace": 1, "p": 2, "P": 2}[option]
+        if i is not None and j is not None:
+            opt = 10 + 3 * (int(i) - 1) + (int(j) - 1)
+        elif option is None:
+            opt = 0
+        else:
+            opt = self._STRESS_OPTIONS.get(option)
+            if opt is None:
+                return np.zeros(ne)
         out = np.zeros(ne * 9 if opt == 0 else ne)
         N.check(self._lib.pfg_element_stress(self._h, N.ptr(d), Ev.shape[0], N.ptr(Ev), N.ptr(vv), opt, N.ptr(out)))
         return out.reshape(ne, 3, 3) if opt == 0 else out

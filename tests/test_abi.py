@@ -95,3 +95,70 @@ def test_ctypes_structs_match_header(cname, pyname):
             (cname, name, pyfield)
         if ctype in sizes:
             assert C.sizeof(pytype) == C.sizeof(sizes[ctype]), (cname, name)
+
+
+# ------------------------------------------------- the Fortran binding module
+F90 = os.path.join(ROOT, "include", "FEMSolverGPUClass.f90")
+_F2C = {"c_int32_t": ("int32_t",), "c_int": ("int32_t", "int"), "c_double": ("double",),
+        "c_int64_t": ("int64_t", "uint64_t"), "c_size_t": ("size_t",)}
+
+
+def _f90_source():
+    return re.sub(r"!.*", "", open(F90).read())  # drop comments
+
+
+def _f90_bindc_types():
+    """{name: [(kind, field), ...]} of the `type, bind(C) :: name` blocks, in order."""
+    out = {}
+    for name, body in re.findall(r"type\s*,\s*bind\(C\)\s*::\s*(\w+)(.*?)end\s+type", _f90_source(), re.S | re.I):
+        fields = []
+        for line in body.strip().splitlines():
+            m = re.match(r"\s*(?:integer|real)\((\w+)\)\s*::\s*(.*)", line)
+            if m:
+                fields += [(m.group(1), f.strip()) for f in m.group(2).split(",")]
+        out[name] = fields
+    return out
+
+
+@pytest.mark.parametrize("cname", ["pfg_solve_opts", "pfg_info", "pfg_eig_opts"])
+def test_fortran_bindc_types_match_header(cname):
+    """The Fortran module's bind(C) types have the header's fields, in order,
+    with interoperable kinds of the same size."""
+    hdr = _header_struct_fields(cname)
+    f90 = _f90_bindc_types()[cname]
+    assert len(hdr) == len(f90), (cname, hdr, f90)
+    for (ctype, name), (kind, fname) in zip(hdr, f90):
+        assert name.lower() == fname.lower(), (cname, name, fname)
+        assert ctype in _F2C[kind], (cname, name, ctype, kind)
+
+
+def _c_prototype_arity():
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for name, args in re.findall(r"\b(pfg_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+        a = args.strip()
+        out[name] = 0 if a in ("", "void") else a.count(",") + 1
+    return out
+
+
+def test_fortran_interfaces_bind_declared_symbols():
+    """Every bind(C, name=...) of the Fortran module names a function that
+    include/pfg.h declares, with as many dummy arguments as the C prototype."""
+    src = _f90_source()
+    ar = _c_prototype_arity()
+    found = re.findall(r"(?:function|subroutine)\s+(\w+)\s*\(([^)]*)\)\s*(?:&\s*)?bind\(C\s*,\s*name\s*=\s*\"(\w+)\"\)",
+                       src, re.I)
+    assert len(found) >= 25
+    for fname, dummies, cname in found:
+        assert fname == cname
+        assert cname in ar, cname
+        n = 0 if not dummies.strip() else dummies.count(",") + 1
+        assert n == ar[cname], (cname, n, ar[cname])
+
+
+def test_fortran_type_bound_names_mirror_femsolver():
+    """FEMSolverGPU_ offers the FEMSolver_ procedures the GPU path covers."""
+    src = _f90_source()
+    bound = set(re.findall(r"procedure\s*,\s*public\s*::\s*(\w+)\s*=>", src, re.I))
+    assert {"init", "setDomain", "setCRS", "setRHS", "setMatrix", "setVector", "fix", "solve", "zeros",
+            "keepThisMatrixAs", "loadMatrix", "fix_eig", "eig", "getCRS", "remove"} <= bound

@@ -86,6 +86,52 @@ def test_element_stress_vs_oracle(cuda):
     np.testing.assert_allclose(I1, np.trace(ref, axis1=1, axis2=2), rtol=0, atol=1e-12 * np.abs(ref).max())
 
 
+def _invariants(S):
+    """The reference's formulas of getElementCauchyStress (FEMDomainClass.f90:15310-15362)."""
+    tr = np.trace(S, axis1=1, axis2=2)
+    I2 = 0.5 * (tr * tr - np.einsum("eij,eji->e", S, S))
+    I3 = np.linalg.det(S)
+    s = S - (tr / 3.0)[:, None, None] * np.eye(3)[None]
+    trs = np.trace(s, axis1=1, axis2=2)
+    J2 = 0.5 * (trs * trs - np.einsum("eij,eji->e", s, s))
+    return {"p": tr / 3.0, "I1": tr, "I2": I2, "I3": I3, "J1": trs, "J2": J2, "J3": np.linalg.det(s)}
+
+
+def test_element_stress_every_option_vs_oracle(cuda):
+    """Every option string of getElementCauchyStress and the (i, j) form,
+    computed on the GPU from the cell-averaged tensors, against the same
+    formulas on the oracle's tensors; an unknown option gives zeros."""
+    dom = FEMDomain().create("Cube3D", 4, 3, 3)
+    rng = np.random.default_rng(3)
+    disp = rng.standard_normal(3 * dom.nn()) * 1e-3
+    E = rng.uniform(1e3, 1e4, dom.ne())
+    nu = rng.uniform(0.1, 0.4, dom.ne())
+    s = FEMSolver()
+    s.setDomain(dom)
+    ref = O.element_stress(dom.nodcoord, dom.elemnod, disp, E, nu)
+    inv = _invariants(ref)
+    scale = np.abs(ref).max()
+    names = {"p": ["p", "P"], "I1": ["I", "I1", "i1", "trace", "tr", "TRACE", "TR"], "I2": ["II", "I2", "i2", "ii"],
+             "I3": ["III", "I3", "i3", "iii"], "J1": ["J", "J1", "j1", "j"], "J2": ["JJ", "J2", "j2", "jj"],
+             "J3": ["JJJ", "J3", "j3", "jjj"]}
+    for key, opts in names.items():
+        tol = 1e-12 * (scale ** (3 if key in ("I3", "J3") else 2 if key in ("I2", "J2") else 1))
+        for o in opts:
+            got = s.getElementCauchyStress(disp, E, nu, option=o)
+            assert np.abs(got - inv[key]).max() <= tol, (o, np.abs(got - inv[key]).max())
+    comps = {"1,1": (0, 0), "2,2": (1, 1), "3,3": (2, 2), "1,2": (0, 1), "2,1": (0, 1), "1,3": (0, 2),
+             "3,1": (0, 2), "3,2": (1, 2), "2,3": (1, 2)}
+    for o, (a, b) in comps.items():
+        for form in (o, f"({o})", "_{" + o + "}"):
+            got = s.getElementCauchyStress(disp, E, nu, option=form)
+            assert np.abs(got - ref[:, a, b]).max() <= 1e-12 * scale, form
+    for a in range(3):
+        for b in range(3):
+            got = s.getElementCauchyStress(disp, E, nu, i=a + 1, j=b + 1)
+            assert np.abs(got - ref[:, a, b]).max() <= 1e-12 * scale, (a, b)
+    assert np.array_equal(s.getElementCauchyStress(disp, E, nu, option="von Mises"), np.zeros(dom.ne()))
+
+
 def test_gravity_bar_stress_kat_gpu(cuda):
     """benchmark_bar_in_gravity_field.f90:56-67 end to end on the GPU:
     I1 of element 1 = -234.026 on the deformed mesh (theory -234.024), with the
