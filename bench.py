@@ -45,7 +45,7 @@ TOL = 1e-10
 # the oracle's own restatement on the CPU (tests/golden/make_config_fixtures.py,
 # stage cfg2_bicgstab; tests/golden/configs/cfg2_bicgstab.npz).  The CPU arm
 # times a bounded sample of iterations and scales by this count.
-REF_ITERS_LOGNORMAL100 = None  # set from the oracle run
+REF_ITERS_LOGNORMAL100 = 1567  # oracle bicgstab_CRS_2 count (true relative residual at exit 9.2e-9)
 # DRAM bytes (read + write) of one k_cg_spmv_u<3,float> launch on lognormal100:
 # an ncu capture on lognormal60 measured dram__bytes_read.sum +
 # dram__bytes_write.sum = 246.4 MB for 244.45 MB of algorithmic bytes (ratio

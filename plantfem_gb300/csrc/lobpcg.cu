@@ -259,6 +259,43 @@ __device__ __forceinline__ const T *panel_row(const T *base, int64_t n, int q, i
     return base + ((int64_t)q * n + row) * PW;
 }
 
+// Double-FP32 ("double-float") arithmetic on the FP32 pipe, for the Gram of
+// the second phase of the mixed LOBPCG: GB300's FP64 pipe is about 1/30 of
+// its FP32 pipe, and the FP64 Gram ran on it at 0.92 TFLOP/s.  (The same form
+// of the SpMM and linear combinations was slower than FP64 there: their
+// operands are split where they are used, a conversion each, where the Gram
+// splits each staged value once for 72 uses.)  Each FP64 value is split into hi + lo floats (exact to
+// 48 bits); a product's rounding error comes exactly from an FMA (Dekker's
+// product), the cross terms hi*lo are added to it, and each sum keeps its
+// rounding error by TwoSum (Knuth); the pair (hi, lo) accumulates one CTA's
+// rows and the partial sums are added in FP64 (Hida, Li & Bailey 2001, "Algorithms
+// for quad-double precision", double-double addition and multiplication).
+// Explicit _rn intrinsics keep the compiler from contracting the error-free
+// steps into FMAs.  Relative error about n_cta * 2^-48 per partial sum.
+struct DFAcc {
+    float hi, lo;
+    __device__ void zero() { hi = lo = 0.f; }
+    __device__ void add(float2 a, float2 b)
+    {
+        const float p = __fmul_rn(a.x, b.x);
+        float e = fmaf(a.x, b.x, -p);
+        e = fmaf(a.x, b.y, e);
+        e = fmaf(a.y, b.x, e);
+        const float t = __fadd_rn(hi, p);
+        const float z = __fsub_rn(t, hi);
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, z)), __fsub_rn(p, z));
+        hi = t;
+        lo = __fadd_rn(lo, __fadd_rn(err, e));
+    }
+    __device__ double get() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ float2 df_split(double x)
+{
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - (double)h));
+}
+
 // Y = A X for every panel (one warp per (slice, panel), one lane per block
 // row); rows of fixed DOFs are zeroed (the reduce_crs_matrix restriction).
 template <int BS, typename T>
@@ -329,6 +366,32 @@ struct GramAcc<float> {
     __device__ double get() const { return (double)v.s + (double)v.c; }
 };
 
+// Staged operand type and accumulator of the Gram kernel per storage type:
+// FP32 panels with compensated FP32 sums, FP64 panels in double-float.
+template <typename T, bool DF>
+struct GramArith;
+template <bool DF>
+struct GramArith<float, DF> {
+    using Stage = float;
+    using Acc = GramAcc<float>;
+    __device__ static float stage(float x) { return x; }
+    __device__ static float none() { return 0.f; }
+};
+template <>
+struct GramArith<double, false> {
+    using Stage = double;
+    using Acc = GramAcc<double>;
+    __device__ static double stage(double x) { return x; }
+    __device__ static double none() { return 0.0; }
+};
+template <>
+struct GramArith<double, true> {
+    using Stage = float2;
+    using Acc = DFAcc;
+    __device__ static float2 stage(double x) { return df_split(x); }
+    __device__ static float2 none() { return make_float2(0.f, 0.f); }
+};
+
 constexpr int kGramRows = 32;  // rows staged in shared memory per step
 constexpr int kGramSub = 4;    // each thread owns a 4 x 4 sub-tile of both Gram matrices
 
@@ -342,11 +405,11 @@ constexpr int kGramSub = 4;    // each thread owns a 4 x 4 sub-tile of both Gram
 // tiles; the upper-triangle tiles (I <= J) are split into four 4 x 4 sub-tiles,
 // one per thread (4 * T (T + 1) / 2 threads for T = m_p / 8 tile columns, at
 // most 312).  Per staged row a thread reads 4 values of S and 4 of each image
-// and does 32 multiply-adds, so the FP64 form runs on the FP64 pipe instead of
-// on shared-memory loads (the former one-pair-per-slot form read 3 values per
-// 2 multiply-adds).  The sub-tile below the diagonal of a diagonal tile is
+// and does 32 multiply-adds: compensated FP32 for FP32 panels, FP64 for FP64
+// panels, or double-float (DF, the mixed mode's second phase) on the FP32
+// pipe, the operands split once when a row is staged.  The sub-tile below the diagonal of a diagonal tile is
 // computed and not written.
-template <typename T>
+template <typename T, bool DF>
 __global__ void __launch_bounds__(320)
     k_gram(int64_t n, int k, int nblk, const T *S0, const T *S1, const T *S2, const T *K0, const T *K1, const T *K2,
            const T *M0, const T *M1, const T *M2, double *part)
@@ -358,9 +421,11 @@ __global__ void __launch_bounds__(320)
     const int npairs = m * (m + 1) / 2;
     const int tiles = mp / PW;
     const int ntasks = kGramSub * tiles * (tiles + 1) / 2;
-    T *sS = (T *)smraw;
-    T *sK = sS + kGramRows * mp;
-    T *sM = sK + kGramRows * mp;
+    using Ar = GramArith<T, DF>;
+    using St = typename Ar::Stage;
+    St *sS = (St *)smraw;
+    St *sK = sS + kGramRows * mp;
+    St *sM = sK + kGramRows * mp;
     const bool active = (int)threadIdx.x < ntasks;
     int i0 = 0, j0 = 0;
     if (active) {
@@ -373,7 +438,7 @@ __global__ void __launch_bounds__(320)
         i0 = PW * I + kGramSub * (sub >> 1);
         j0 = PW * (I + rem) + kGramSub * (sub & 1);
     }
-    GramAcc<T> aA[kGramSub][kGramSub], aB[kGramSub][kGramSub];
+    typename Ar::Acc aA[kGramSub][kGramSub], aB[kGramSub][kGramSub];
 #pragma unroll
     for (int a = 0; a < kGramSub; ++a)
 #pragma unroll
@@ -394,14 +459,14 @@ __global__ void __launch_bounds__(320)
             const int q = cc / PW, c = cc - q * PW;
             const int64_t off = ((int64_t)q * n + t0 + r) * PW + c;
             const bool real = cc < k;
-            sS[r * mp + col] = real ? SS[b][off] : T(0);
-            sK[r * mp + col] = real ? KK[b][off] : T(0);
-            sM[r * mp + col] = real ? MM[b][off] : T(0);
+            sS[r * mp + col] = real ? Ar::stage(SS[b][off]) : Ar::none();
+            sK[r * mp + col] = real ? Ar::stage(KK[b][off]) : Ar::none();
+            sM[r * mp + col] = real ? Ar::stage(MM[b][off]) : Ar::none();
         }
         __syncthreads();
         if (active) {
             for (int r = 0; r < rows; ++r) {
-                T si[kGramSub], yk[kGramSub], ym[kGramSub];
+                St si[kGramSub], yk[kGramSub], ym[kGramSub];
 #pragma unroll
                 for (int a = 0; a < kGramSub; ++a) {
                     si[a] = sS[r * mp + i0 + a];
@@ -654,6 +719,7 @@ struct Ctx {
     int k, kp, np;
     cudaStream_t st;
     const uint8_t *fixed;
+    bool df = false;  // the Gram of FP64 panels in double-float (the mixed mode's second phase)
     int launches = 0;
     DevBuf<double> part, gram, C, lam_d, dinv;
     std::vector<double> hg, hC, hlam;
@@ -696,13 +762,14 @@ void gram(Ctx &c, int nblk, const Blocks<T> &B, std::vector<double> &GA, std::ve
     const int mp = nblk * c.kp;
     const int tiles = mp / PW;
     const int threads = (kGramSub * tiles * (tiles + 1) / 2 + 31) / 32 * 32;
-    const size_t smem = (size_t)3 * kGramRows * mp * sizeof(T);
+    const size_t smem = (size_t)3 * kGramRows * mp * sizeof(T);  // (a double-float operand is 8 bytes too)
     const int g = c.ngrid;
     c.part.ensure((size_t)g * 2 * npairs);
     c.gram.ensure((size_t)2 * npairs);
-    PFG_CUDA(cudaFuncSetAttribute(k_gram<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_gram<T><<<g, threads, smem, c.st>>>(c.n, c.k, nblk, B.X.p, B.W.p, B.P.p, B.KX.p, B.KW.p, B.KP.p, B.MX.p,
-                                          B.MW.p, B.MP.p, c.part.p);
+    auto kern = (std::is_same<T, double>::value && c.df) ? k_gram<T, true> : k_gram<T, false>;
+    PFG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<g, threads, smem, c.st>>>(c.n, c.k, nblk, B.X.p, B.W.p, B.P.p, B.KX.p, B.KW.p, B.KP.p, B.MX.p, B.MW.p,
+                                     B.MP.p, c.part.p);
     k_reduce_parts<<<grid_for(2 * npairs, 256, 64), 256, 0, c.st>>>(c.part.p, g, 2 * npairs, c.gram.p);
     PFG_CUDA(cudaGetLastError());
     c.launches += 2;
@@ -942,6 +1009,9 @@ EigResult lobpcg_solve(DevMatrix &K, DevMatrix &M, const uint8_t *fixed, const E
         ++c.launches;
         start = 1;
     }
+    // the mixed mode's second phase: FP64 panels, the Gram in double-float on
+    // the FP32 pipe; precision FP64: IEEE FP64 throughout
+    c.df = cfg.precision == PFG_PREC_MIXED;
     rc = phase<double>(c, K, M, B64, cfg, false, start, iters_left, iters_done, max_rel, ref_r1);
     res.iterations = iters_done;
     res.max_rel_residual = max_rel;
