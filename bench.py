@@ -206,8 +206,9 @@ def run_ours(args, ws, rank, local):
     infos = []
     torch.cuda.synchronize()
     ev0.record()
-    for _ in range(args.steps):
-        infos.append(solve_once("mixed"))
+    with _nvtx("timed_mixed"):  # profiler filter (ncu --nvtx-include)
+        for _ in range(args.steps):
+            infos.append(solve_once("mixed"))
     ev1.record()
     torch.cuda.synchronize()
     ms_total = ev0.elapsed_time(ev1)
@@ -288,8 +289,9 @@ def bicgstab_lines(s, b, x):
         # FP32 inner iterations from the upper-triangle copy, transposes summed
         # in fixed point: bitwise reproducible, so three runs agree to the bit
         # (iterations and time spread reported)
-        sym = [run(preconditioning="BlockJacobi", precision="mixed", stop_rule="true_relative",
-                   reliable_delta=0.1, storage="symmetric") for _ in range(3)]
+        with _nvtx("bicgstab_sym"):  # profiler filter (ncu --nvtx-include)
+            sym = [run(preconditioning="BlockJacobi", precision="mixed", stop_rule="true_relative",
+                       reliable_delta=0.1, storage="symmetric") for _ in range(3)]
         ok = sorted((r["ms"], k) for k, r in enumerate(sym) if "ms" in r)
         its = [r["iterations"] for r in sym if "iterations" in r]
         out["block_jacobi_mixed_symmetric_delta_0.1"] = {
