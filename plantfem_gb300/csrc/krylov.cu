@@ -941,10 +941,11 @@ __global__ void __launch_bounds__(kThreads)
 // form serves the mixed CG, whose iteration count does not follow those bits
 // (1841-1842 iterations on the 3.09M-DOF system); the mixed BiCGSTAB, whose
 // count does, uses the reproducible fixed-point form below.
+// (no "memory" clobber: the kernels that use it never read the accumulator, so
+// the compiler may keep issuing the next slots' loads across a reduction)
 __device__ __forceinline__ void red_add_v4(float *a, float x, float y, float z)
 {
-    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(0.f)
-                 : "memory");
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(0.f));
 }
 
 // y4 += A x from the upper half U (y4: 4 floats per block row, zero on entry)
@@ -992,11 +993,10 @@ __global__ void __launch_bounds__(kThreads)
 // fin: alpha = rho / <p, Ap>.  With acc_i = sum over the row's stored blocks
 // (j >= i) of A_ij p_j, symmetry gives <p, Ap> = sum_i (2 p_i.acc_i - p_i^T A_ii p_i),
 // so the reduction does not wait for the scattered transposes.
-// 5 CTAs per SM (<= 51 registers) with the slot loop not unrolled: measured
-// 104 us per launch at 3.09M DOF vs 129 us at the default 58 registers.
-__global__ void __launch_bounds__(kThreads, 5)
-    k_cg_spmv_sym(SellView<float> U, const float *__restrict__ p, float *__restrict__ q4, KState *S, double *pd,
-                  float *pf, unsigned *ticket)
+template <int UNR, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+    k_cg_spmv_sym_t(SellView<float> U, const float *__restrict__ p, float *__restrict__ q4, KState *S, double *pd,
+                    float *pf, unsigned *ticket)
 {
     if (S->done | S->need_update) return;
     Comp32 dot[1] = {Comp32{0.f, 0.f}};
@@ -1012,7 +1012,7 @@ __global__ void __launch_bounds__(kThreads, 5)
         const int *cp = U.col + b0 * 32 + lane;
         const float *vp = U.val + b0 * 32 * 9 + lane;
         float acc[3] = {0.f, 0.f, 0.f}, dg[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
+#pragma unroll UNR
         for (int k = 0; k < w; ++k) {
             const int c = ld_stream(cp + (int64_t)k * 32);
             float a[9];
@@ -1057,6 +1057,12 @@ __global__ void __launch_bounds__(kThreads, 5)
     }
 }
 
+// The configuration the solves use.  Measured per launch at 3.09M DOF: two
+// slots per loop step at 4 CTAs per SM (63 registers) 0.1015 ms; one slot at 5
+// CTAs (47 registers) 0.1036 ms, at 6 CTAs (40) 0.135 ms; three slots at 3 CTAs
+// 0.107 ms; two at 3 CTAs 0.109 ms.
+#define k_cg_spmv_sym k_cg_spmv_sym_t<2, 4>
+
 // Reproducible form of the symmetric product (the BiCGSTAB inner iterations,
 // whose iteration count follows every rounding difference).  Each row's own
 // stored blocks are summed in FP32 by the lane that owns the row, in slot
@@ -1088,9 +1094,10 @@ __device__ __forceinline__ int symfx_exponent(float rowsum, unsigned xmax_bits)
 // y = (own stored blocks) x; acc64[t nb + c] += fixed-point transposes (three
 // planes: a warp's reductions of one component cover consecutive words; the
 // three components of a row in one sector made the reductions twice as slow)
-__global__ void __launch_bounds__(kThreads, 5)
-    k_spmv_symfx(SellView<float> U, const float *__restrict__ x, float *__restrict__ y,
-                 unsigned long long *__restrict__ acc64, float rowsum, const KState *S)
+template <int UNR, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+    k_spmv_symfx_t(SellView<float> U, const float *__restrict__ x, float *__restrict__ y,
+                   unsigned long long *__restrict__ acc64, float rowsum, const KState *S)
 {
     if (S->done | S->need_update) return;
     const float scale = exp2f((float)symfx_exponent(rowsum, S->xmax_bits));
@@ -1106,7 +1113,7 @@ __global__ void __launch_bounds__(kThreads, 5)
         const int *cp = U.col + b0 * 32 + lane;
         const float *vp = U.val + b0 * 32 * 9 + lane;
         float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
+#pragma unroll UNR
         for (int k = 0; k < w; ++k) {
             const int c = ld_stream(cp + (int64_t)k * 32);
             float a[9];
@@ -1130,6 +1137,9 @@ __global__ void __launch_bounds__(kThreads, 5)
             for (int t = 0; t < 3; ++t) y[3 * row + t] = acc[t];
     }
 }
+// one slot per loop step at 5 CTAs per SM: 0.113 ms per launch at 3.09M DOF
+// (two slots at 4 CTAs: 0.127 ms)
+#define k_spmv_symfx k_spmv_symfx_t<1, 5>
 
 // y += acc64 / scale (acc64 = 0 for the next product), then the dot products
 // and scalar updates of the BiCGSTAB products:
@@ -2215,7 +2225,7 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
         y32.alloc((size_t)n);
         k_fill<<<gv, 256, 0, st>>>(x32.p, n, 1.0f);
         bytes = (double)A.nnzb * bs2 * 4.0 + idx + 2.0 * (double)n * 4.0;
-        if (kernel >= 7)  // the upper half: (nnzb + nb) / 2 blocks of a symmetric pattern
+        if (kernel >= 7 && kernel != 9)  // the upper half: (nnzb + nb) / 2 blocks of a symmetric pattern
             bytes = (double)(A.nnzb + A.nb) / 2.0 * (bs2 * 4.0 + 4.0) + (double)(A.nb + 1) * 8.0 +
                     2.0 * (double)n * 4.0;
         if (kernel == 2) {
