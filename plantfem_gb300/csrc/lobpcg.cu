@@ -259,12 +259,10 @@ __device__ __forceinline__ const T *panel_row(const T *base, int64_t n, int q, i
     return base + ((int64_t)q * n + row) * PW;
 }
 
-// Double-FP32 ("double-float") arithmetic on the FP32 pipe, for the Gram of
-// the second phase of the mixed LOBPCG: GB300's FP64 pipe is about 1/30 of
-// its FP32 pipe, and the FP64 Gram ran on it at 0.92 TFLOP/s.  (The same form
-// of the SpMM and linear combinations was slower than FP64 there: their
-// operands are split where they are used, a conversion each, where the Gram
-// splits each staged value once for 72 uses.)  Each FP64 value is split into hi + lo floats (exact to
+// Double-FP32 ("double-float") arithmetic on the FP32 pipe, for the second
+// phase of the mixed LOBPCG (its Gram, SpMM and linear combinations of FP64
+// panels): GB300's FP64 pipe is about 1/30 of its FP32 pipe, and the FP64
+// forms of these kernels ran on it (the Gram at 0.92 TFLOP/s).  Each FP64 value is split into hi + lo floats (exact to
 // 48 bits); a product's rounding error comes exactly from an FMA (Dekker's
 // product), the cross terms hi*lo are added to it, and each sum keeps its
 // rounding error by TwoSum (Knuth); the pair (hi, lo) accumulates one CTA's
@@ -349,6 +347,127 @@ __global__ void __launch_bounds__(kT) k_spmm(SellView<T> A, int np, const T *__r
     }
 }
 
+// ---- double-float forms of the SpMM and the linear combinations (mixed
+// second phase).  Their operands are converted to (hi, lo) float pairs in one
+// pass each (k_to_df: one FP64 subtraction per value), so the inner loops are
+// FP32 arithmetic only; splitting each operand where it is used put a
+// conversion per use on the FP64 pipe and was slower than FP64 itself.
+__global__ void k_to_df(int64_t len, const double *__restrict__ a, float2 *__restrict__ b)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
+        b[i] = df_split(a[i]);
+}
+
+// Y = A X with A's sliced values (vdf, A's slot layout) and the panels X in
+// double-float; Y in FP64.  Layout and warp mapping as k_spmm.
+template <int BS>
+__global__ void __launch_bounds__(kT) k_spmm_df(SellView<double> A, const float2 *__restrict__ vdf, int np,
+                                                const float2 *__restrict__ X, double *__restrict__ Y,
+                                                const uint8_t *__restrict__ fixed)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t n = A.nb * BS;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = w0; u < A.ns * np; u += nw) {
+        const int64_t s = u / np;
+        const int q = (int)(u - s * np);
+        const int64_t b0 = A.sptr[s];
+        const int wdt = (int)(A.sptr[s + 1] - b0);
+        const int *cp = A.col + b0 * 32 + lane;
+        const float2 *vp = vdf + b0 * 32 * (BS * BS) + lane;
+        DFAcc acc[BS][PW];
+#pragma unroll
+        for (int r = 0; r < BS; ++r)
+#pragma unroll
+            for (int c = 0; c < PW; ++c) acc[r][c].zero();
+        for (int k = 0; k < wdt; ++k) {
+            const int col = ld_stream(cp + (int64_t)k * 32);
+            float2 a[BS * BS];
+#pragma unroll
+            for (int e = 0; e < BS * BS; ++e) a[e] = __ldg(vp + ((int64_t)k * (BS * BS) + e) * 32);
+#pragma unroll
+            for (int cc = 0; cc < BS; ++cc) {
+                const float2 *xr = panel_row(X, n, q, (int64_t)BS * col + cc);
+                float2 xv[PW];
+#pragma unroll
+                for (int c = 0; c < PW; ++c) xv[c] = __ldg(xr + c);
+#pragma unroll
+                for (int r = 0; r < BS; ++r)
+#pragma unroll
+                    for (int c = 0; c < PW; ++c) acc[r][c].add(a[r * BS + cc], xv[c]);
+            }
+        }
+        const int64_t row = s * 32 + lane;
+        if (row < A.nb) {
+#pragma unroll
+            for (int r = 0; r < BS; ++r) {
+                const int64_t i = (int64_t)BS * row + r;
+                const bool f = fixed && fixed[i];
+                double *yr = Y + ((int64_t)q * n + i) * PW;
+#pragma unroll
+                for (int c = 0; c < PW; ++c) yr[c] = f ? 0.0 : acc[r][c].get();
+            }
+        }
+    }
+}
+
+// k_lincomb with the blocks and the coefficients in double-float; outputs FP64.
+__global__ void __launch_bounds__(kT)
+    k_lincomb_df(int64_t n, int k, int nblk, const float2 *__restrict__ X, const float2 *__restrict__ W,
+                 const float2 *__restrict__ P, const double *__restrict__ C, double *__restrict__ Xn,
+                 double *__restrict__ Pn)
+{
+    extern __shared__ unsigned char smraw[];
+    float2 *sC = (float2 *)smraw;
+    const int m = nblk * k;
+    const int np = (k + PW - 1) / PW;
+    for (int i = threadIdx.x; i < m * k; i += blockDim.x) sC[i] = df_split(C[i]);
+    __syncthreads();
+    const float2 *B[3] = {X, W, P};
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+        for (int qo = 0; qo < np; ++qo) {
+            DFAcc ax[PW], ap[PW];
+#pragma unroll
+            for (int c = 0; c < PW; ++c) {
+                ax[c].zero();
+                ap[c].zero();
+            }
+            for (int b = 0; b < nblk; ++b) {
+                for (int qi = 0; qi < np; ++qi) {
+                    const float2 *src = panel_row(B[b], n, qi, row);
+                    float2 v[PW];
+#pragma unroll
+                    for (int c = 0; c < PW; ++c) v[c] = src[c];
+#pragma unroll
+                    for (int c = 0; c < PW; ++c) {
+                        const int i = qi * PW + c;
+                        if (i >= k) break;
+                        const float2 *crow = sC + (b * k + i);
+#pragma unroll
+                        for (int o = 0; o < PW; ++o) {
+                            const int jj = qo * PW + o;
+                            const float2 cij = jj < k ? crow[(int64_t)jj * m] : make_float2(0.f, 0.f);
+                            if (b == 0)
+                                ax[o].add(v[c], cij);
+                            else
+                                ap[o].add(v[c], cij);
+                        }
+                    }
+                }
+            }
+            double *xo = Xn + ((int64_t)qo * n + row) * PW;
+            double *po = Pn + ((int64_t)qo * n + row) * PW;
+#pragma unroll
+            for (int o = 0; o < PW; ++o) {
+                const double pv = ap[o].get();
+                po[o] = pv;
+                xo[o] = ax[o].get() + pv;
+            }
+        }
+    }
+}
+
 template <typename T>
 struct GramAcc;
 template <>
@@ -370,10 +489,19 @@ struct GramAcc<float> {
 // FP32 panels with compensated FP32 sums, FP64 panels in double-float.
 template <typename T, bool DF>
 struct GramArith;
+// FP32 panels (the mixed first phase, which stops at a 1e-4 residual): plain
+// FP32 multiply-adds per thread over its CTA's rows (about n / 300 terms),
+// partial sums added in FP64.  DF = true keeps the compensated FP32 form.
+struct F32Acc {
+    float v;
+    __device__ void zero() { v = 0.f; }
+    __device__ void add(float a, float b) { v = fmaf(a, b, v); }
+    __device__ double get() const { return (double)v; }
+};
 template <bool DF>
 struct GramArith<float, DF> {
     using Stage = float;
-    using Acc = GramAcc<float>;
+    using Acc = typename std::conditional<DF, GramAcc<float>, F32Acc>::type;
     __device__ static float stage(float x) { return x; }
     __device__ static float none() { return 0.f; }
 };
@@ -719,7 +847,9 @@ struct Ctx {
     int k, kp, np;
     cudaStream_t st;
     const uint8_t *fixed;
-    bool df = false;  // the Gram of FP64 panels in double-float (the mixed mode's second phase)
+    bool df = false;  // FP64 panels: Gram, SpMM and linear combinations in double-float (mixed second phase)
+    DevBuf<float2> df_a, df_b, df_c, df_K, df_M;  // converted panels (3) and sliced matrix values
+    const DevMatrix *dfK = nullptr, *dfM = nullptr;
     int launches = 0;
     DevBuf<double> part, gram, C, lam_d, dinv;
     std::vector<double> hg, hC, hlam;
@@ -733,6 +863,59 @@ SellView<T> sell_of(const DevMatrix &A)
         return A.sell<double>();
     else
         return A.sell<float>();
+}
+
+// A's sliced FP64 values as double-float pairs (converted once per phase).
+static const float2 *df_values(Ctx &c, const DevMatrix &A)
+{
+    const bool isK = &A == c.dfK;
+    PFG_CHECK(isK || &A == c.dfM, PFG_E_INTERNAL, "double-float values of an unexpected matrix");
+    return isK ? c.df_K.p : c.df_M.p;
+}
+
+static void to_df(Ctx &c, const double *a, float2 *b, int64_t len)
+{
+    k_to_df<<<grid_for(len, 256, sms() * 8), 256, 0, c.st>>>(len, a, b);
+    PFG_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+// Y = A X for X already in double-float (Xdf).
+static void spmm_df(Ctx &c, const DevMatrix &A, const float2 *Xdf, double *Y)
+{
+    const SellView<double> v = A.sell<double>();
+    int per = 0;
+    if (A.bs == 3)
+        PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm_df<3>, kT, 0));
+    else
+        PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm_df<1>, kT, 0));
+    const int64_t warps = A.ns * c.np;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)std::max(per, 1) * sms()));
+    if (A.bs == 3)
+        k_spmm_df<3><<<g, kT, 0, c.st>>>(v, df_values(c, A), c.np, Xdf, Y, c.fixed);
+    else
+        k_spmm_df<1><<<g, kT, 0, c.st>>>(v, df_values(c, A), c.np, Xdf, Y, c.fixed);
+    PFG_CUDA(cudaGetLastError());
+    ++c.launches;
+}
+
+template <typename T>
+void spmm(Ctx &c, const DevMatrix &A, const T *X, T *Y);
+
+// KX = K X and MX = M X (X converted once in double-float mode).
+template <typename T>
+void spmm_pair(Ctx &c, const DevMatrix &K, const DevMatrix &M, const T *X, T *KX, T *MX)
+{
+    if constexpr (std::is_same<T, double>::value) {
+        if (c.df) {
+            to_df(c, X, c.df_a.p, c.n * c.kp);
+            spmm_df(c, K, c.df_a.p, KX);
+            spmm_df(c, M, c.df_a.p, MX);
+            return;
+        }
+    }
+    spmm<T>(c, K, X, KX);
+    spmm<T>(c, M, X, MX);
 }
 
 template <typename T>
@@ -791,6 +974,20 @@ void lincomb(Ctx &c, int nblk, const T *X, const T *W, const T *P, T *Xn, T *Pn)
 {
     const int m = nblk * c.k;
     const size_t smem = (size_t)m * c.k * sizeof(T);
+    if constexpr (std::is_same<T, double>::value) {
+        if (c.df) {  // float2 coefficients: the same 8 bytes each
+            const int64_t len = c.n * c.kp;
+            to_df(c, X, c.df_a.p, len);
+            to_df(c, W, c.df_b.p, len);
+            if (nblk == 3) to_df(c, P, c.df_c.p, len);
+            PFG_CUDA(cudaFuncSetAttribute(k_lincomb_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k_lincomb_df<<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, c.df_a.p, c.df_b.p,
+                                                                          c.df_c.p, c.C.p, Xn, Pn);
+            PFG_CUDA(cudaGetLastError());
+            ++c.launches;
+            return;
+        }
+    }
     PFG_CUDA(cudaFuncSetAttribute(k_lincomb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_lincomb<T><<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, X, W, P, c.C.p, Xn, Pn);
     PFG_CUDA(cudaGetLastError());
@@ -933,8 +1130,7 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
                                                                                 B.R.p, B.W.p, c.fixed);
         PFG_CUDA(cudaGetLastError());
         ++c.launches;
-        spmm<T>(c, K, B.W.p, B.KW.p);
-        spmm<T>(c, M, B.W.p, B.MW.p);
+        spmm_pair<T>(c, K, M, B.W.p, B.KW.p, B.MW.p);
         int nblk = haveP ? 3 : 2;
         int got = rayleigh_ritz<T>(c, nblk, B, rank_tol);
         if (got < c.k && nblk == 3) {
@@ -951,10 +1147,8 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
         // phase stalled near 3e-3 on the 60^3 cantilever).
         if (++since_refresh >= kRefreshImages) {
             since_refresh = 0;
-            spmm<T>(c, K, B.X.p, B.KX.p);
-            spmm<T>(c, M, B.X.p, B.MX.p);
-            spmm<T>(c, K, B.P.p, B.KP.p);
-            spmm<T>(c, M, B.P.p, B.MP.p);
+            spmm_pair<T>(c, K, M, B.X.p, B.KX.p, B.MX.p);
+            spmm_pair<T>(c, K, M, B.P.p, B.KP.p, B.MP.p);
         }
     }
 }
@@ -1009,9 +1203,21 @@ EigResult lobpcg_solve(DevMatrix &K, DevMatrix &M, const uint8_t *fixed, const E
         ++c.launches;
         start = 1;
     }
-    // the mixed mode's second phase: FP64 panels, the Gram in double-float on
-    // the FP32 pipe; precision FP64: IEEE FP64 throughout
+    // the mixed mode's second phase: FP64 panels, their SpMM, Gram and linear
+    // combinations in double-float on the FP32 pipe; precision FP64: IEEE FP64
     c.df = cfg.precision == PFG_PREC_MIXED;
+    if (c.df) {
+        const int64_t len = c.n * c.kp;
+        c.df_a.resize((size_t)len);
+        c.df_b.resize((size_t)len);
+        c.df_c.resize((size_t)len);
+        c.dfK = &K;
+        c.dfM = &M;
+        c.df_K.resize(K.s64.n);
+        c.df_M.resize(M.s64.n);
+        to_df(c, K.s64.p, c.df_K.p, (int64_t)K.s64.n);
+        to_df(c, M.s64.p, c.df_M.p, (int64_t)M.s64.n);
+    }
     rc = phase<double>(c, K, M, B64, cfg, false, start, iters_left, iters_done, max_rel, ref_r1);
     res.iterations = iters_done;
     res.max_rel_residual = max_rel;
