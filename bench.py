@@ -52,9 +52,10 @@ REF_ITERS_LOGNORMAL100 = 1567  # oracle bicgstab_CRS_2 count (true relative resi
 # 1.008), applied to the 1.1238 GB of the 100^3 launch (the kernel's traffic
 # grows in proportion to the blocks it streams).
 TRAFFIC_CG_SPMV_FP32 = 1.1328e9
-# The same for k_cg_spmv_sym (the upper half): 134.2 MB measured for 130.4 MB
-# algorithmic on lognormal60 (ratio 1.029), applied to the 599.0 MB at 100^3.
-TRAFFIC_CG_SPMV_SYM = 6.164e8
+# The same for k_cg_spmv_symb (the upper half, bulk-staged): 134.2 MB measured
+# for 130.4 MB algorithmic on lognormal60 (ratio 1.030), applied to the
+# 599.0 MB at 100^3.
+TRAFFIC_CG_SPMV_SYM = 6.167e8
 # FP32 copy the headline mixed solve reads: "symmetric" (upper half of the
 # symmetric matrix, half the bytes) or "full".
 STORAGE = "symmetric"
@@ -620,13 +621,15 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
     from plantfem_gb300 import _native, linear_solver_crs
     # kernel roofline: the dominant kernel of the mixed solve is the FP32
     # product from the upper half of the symmetric matrix with the fused
-    # p.Ap reduction, k_cg_spmv_sym (with the full copy: k_cg_spmv_u<3,float>);
+    # p.Ap reduction, k_cg_spmv_symb (matrix planes staged in shared memory by
+    # bulk copies; with the full copy: k_cg_spmv_u<3,float>);
     # each is timed with CUDA events on the handle's stream over 20
     # back-to-back launches
     import ctypes as C
     prof = {}
     for kid, name in ((0, "spmv_fp64"), (1, "spmv_fp32"), (2, "cg_spmv_fp32_fused"), (5, "cg_spmv_fp32"),
-                      (6, "cg_spmv_fp64"), (7, "spmv_fp32_symmetric"), (8, "cg_spmv_fp32_symmetric")):
+                      (6, "cg_spmv_fp64"), (7, "spmv_fp32_symmetric"), (8, "cg_spmv_fp32_symmetric"),
+                      (11, "cg_spmv_fp32_symmetric_unstaged")):
         ms, by = C.c_double(), C.c_double()
         _native.check(_native.load().pfg_profile_kernel(s.handle, kid, 20, C.byref(ms), C.byref(by)))
         prof[name] = {"ms": ms.value, "bytes": by.value, "GBs": by.value / (ms.value * 1e-3) / 1e9}
@@ -634,7 +637,8 @@ def run_rest(args, ws, rank, s, b, x, x64_host, ndof, n, infos, mixed_info, err_
     peak = pk["hbm_gbs"] if pk else 6800.0
     sym = STORAGE == "symmetric"
     dom_k = prof["cg_spmv_fp32_symmetric" if sym else "cg_spmv_fp32"]
-    roofline = {"kernel": ("k_cg_spmv_sym (FP32 product from the upper 3x3 blocks of the symmetric matrix + p.Ap)"
+    roofline = {"kernel": ("k_cg_spmv_symb (FP32 product from the upper 3x3 blocks of the symmetric matrix + p.Ap, "
+                           "bulk-staged)"
                            if sym else "k_cg_spmv_u<3,float> (FP32 3x3-block SELL SpMV + p.q)"), "bound": "hbm",
                 "achieved": round(dom_k["GBs"], 1), "peak": peak, "unit": "GB/s",
                 "frac": round(dom_k["GBs"] / peak, 4),

@@ -457,13 +457,16 @@ int pfg_batch_abort_flag(pfg_batch *b, volatile int32_t **flag);
  * CG SpMV with the p.q reduction (the dominant kernels of the mixed and FP64
  * solves with streaming update passes, the default), 7 = the FP32 product from
  * the upper half of a symmetric matrix (PFG_STORAGE_SYMMETRIC), 8 = its CG form
- * with the fused p.Ap (the dominant kernel of the symmetric-storage mixed CG),
- * 9 = one D^-1 L^-1 sweep of the held ILU(0) factor (all its level launches;
- * the factor is taken in ascending column order first if none is held),
- * 10 = the reproducible FP32 symmetric product of the mixed BiCGSTAB (own
- * blocks in FP32, transposes in 64-bit fixed point; its finish pass is not
- * part of the launch).  Kernels 2, 5, 6 and 8 need a symmetric positive
- * definite (eliminated) matrix, 7 and 10 a symmetric one. */
+ * with the fused p.Ap (the dominant kernel of the symmetric-storage mixed CG:
+ * matrix planes staged in shared memory by bulk copies), 9 = one D^-1 L^-1
+ * sweep of the held ILU(0) factor (all its level launches; the factor is taken
+ * in ascending column order first if none is held), 10 = the reproducible FP32
+ * symmetric product of the mixed BiCGSTAB (own blocks in FP32, transposes in
+ * 64-bit fixed point, matrix planes staged like 8's; its finish pass is not
+ * part of the launch), 11 / 12 = kernels 8 / 10 in their register-pipelined
+ * form (no staging; for comparison).  Kernels 2, 5, 6, 8 and 11 need a
+ * symmetric positive definite (eliminated) matrix, 7, 10 and 12 a symmetric
+ * one. */
 int pfg_profile_kernel(pfg_solver *h, int32_t kernel, int32_t reps, double *ms_per_launch, double *bytes_per_launch);
 
 #ifdef __cplusplus

@@ -25,6 +25,7 @@
 
 #include "krylov.cuh"
 #include "ilu.cuh"
+#include "bulk.cuh"
 
 namespace pfg {
 
@@ -1057,11 +1058,260 @@ __global__ void __launch_bounds__(kThreads, MINB)
     }
 }
 
-// The configuration the solves use.  Measured per launch at 3.09M DOF: two
-// slots per loop step at 4 CTAs per SM (63 registers) 0.1015 ms; one slot at 5
-// CTAs (47 registers) 0.1036 ms, at 6 CTAs (40) 0.135 ms; three slots at 3 CTAs
-// 0.107 ms; two at 3 CTAs 0.109 ms.
-#define k_cg_spmv_sym k_cg_spmv_sym_t<2, 4>
+// Register-pipelined form (loads of two slots per loop step in flight,
+// 63 registers, 4 CTAs per SM): 0.1015-0.1036 ms per launch at 3.09M DOF, kept
+// as a profiling reference for the bulk-staged form below that the solves use.
+// (One slot at 5 CTAs: 0.1036 ms; three slots at 3 CTAs: 0.107 ms; an L2
+// evict-first policy on its loads: 0.117 ms.)
+
+// Bulk-staged form of the CG product, the one the solves use.  The column
+// and value planes of a warp's slices are streamed into a ring of NST
+// shared-memory stages of CH slots each by the bulk copy engine
+// (cp.async.bulk, completion counted on one mbarrier per stage), so the bytes
+// in flight no longer depend on how many loads the warp's registers can hold;
+// the lanes read the staged planes (consecutive lanes, consecutive words: no
+// bank conflicts) and gather p as above.  A slot of a slice is 32 columns
+// (128 B) and 9 x 32 values (1152 B), contiguous in the sliced layout, so a
+// stage is two copies.  The copies carry an L2 evict-first policy: the
+// streamed matrix (0.6 GB at 3.09M DOF) then leaves p and the accumulator
+// (29 MB) resident in L2 for the gathers and the transposed reductions.  A
+// stage that does not complete within the wait limit stops the warp with
+// PFG_E_INTERNAL (after waiting, again bounded, for its copies in flight).
+// Measured per launch at 3.09M DOF (GB300): CH 2, NST 4 (82 KB of stages per
+// CTA, 2 CTAs per SM) 0.0959 ms; CH 3, NST 3: 0.098 ms; CH 4, NST 2: 0.100 ms;
+// CH 2, NST 5: 0.101 ms; CH 1, NST 6: 0.104 ms; CH 2, NST 4 without the L2
+// policy: 0.102 ms.
+template <int CH, int NST>
+struct SymBulk {
+    static constexpr int kColB = CH * 32 * 4;
+    static constexpr int kValB = CH * 32 * 9 * 4;
+    static constexpr int kStageB = kColB + kValB;
+    static constexpr int kBarB = ((kWarps * NST * 8 + 127) / 128) * 128;
+    static constexpr int kSmem = kBarB + kWarps * NST * kStageB;
+};
+
+// One warp's ring of stages over the slices w0, w0 + nw, ... of U (empty
+// slices skipped).  Chunks are consumed in the order they are produced:
+// chunk c sits in stage c % NST, and its barrier completes phase c / NST.
+template <int CH, int NST, bool EVF>
+struct SliceStager {
+    using L = SymBulk<CH, NST>;
+    SellView<float> U;
+    uint64_t *bar;
+    unsigned char *stages;
+    int64_t nw, ps, pb0;
+    int pw, pk, lane;
+    unsigned pidx, cidx;
+    uint64_t pol;
+
+    __device__ void init(unsigned char *dsm, const SellView<float> &u, int64_t w0, int64_t nw_)
+    {
+        U = u;
+        lane = threadIdx.x & 31;
+        const int wid = threadIdx.x >> 5;
+        bar = reinterpret_cast<uint64_t *>(dsm) + wid * NST;
+        stages = dsm + L::kBarB + (size_t)wid * NST * L::kStageB;
+        if (lane == 0) {
+#pragma unroll
+            for (int i = 0; i < NST; ++i) mbar_init(bar + i, 1);
+            fence_proxy_async_smem();
+        }
+        __syncwarp();
+        pol = EVF ? l2_evict_first_policy() : 0ull;
+        nw = nw_;
+        ps = w0;
+        pidx = cidx = 0;
+        seek();
+#pragma unroll
+        for (int i = 0; i < NST; ++i) produce();
+    }
+    __device__ void seek()  // first non-empty slice at or after ps
+    {
+        for (; ps < U.ns; ps += nw) {
+            pb0 = U.sptr[ps];
+            pw = (int)(U.sptr[ps + 1] - pb0);
+            if (pw > 0) break;
+        }
+        pk = 0;
+    }
+    __device__ void produce()
+    {
+        if (ps >= U.ns) return;
+        const int st = (int)(pidx % NST);
+        const int nsl = min(CH, pw - pk);
+        if (lane == 0) {
+            unsigned char *dst = stages + st * L::kStageB;
+            const int *cs = U.col + (pb0 + pk) * 32;
+            const float *vs = U.val + (pb0 + pk) * 288;
+            mbar_arrive_expect_tx(bar + st, (unsigned)nsl * 1280u);
+            if (EVF) {
+                bulk_g2s_hint(dst, cs, (unsigned)nsl * 128u, bar + st, pol);
+                bulk_g2s_hint(dst + L::kColB, vs, (unsigned)nsl * 1152u, bar + st, pol);
+            } else {
+                bulk_g2s(dst, cs, (unsigned)nsl * 128u, bar + st);
+                bulk_g2s(dst + L::kColB, vs, (unsigned)nsl * 1152u, bar + st);
+            }
+        }
+        ++pidx;
+        pk += nsl;
+        if (pk >= pw) {
+            ps += nw;
+            seek();
+        }
+    }
+    // Waits for the next chunk (false: it did not complete within the limit).
+    __device__ bool wait(const int *&cols, const float *&vals)
+    {
+        const int st = (int)(cidx % NST);
+        if (!__all_sync(0xffffffffu, mbar_wait(bar + st, (cidx / NST) & 1u))) return false;
+        cols = reinterpret_cast<const int *>(stages + st * L::kStageB);
+        vals = reinterpret_cast<const float *>(stages + st * L::kStageB + L::kColB);
+        return true;
+    }
+    // Every lane has read the chunk: refill its stage with the next one.
+    __device__ void release()
+    {
+        __syncwarp();
+        if (lane == 0) fence_proxy_async_smem();
+        produce();
+        ++cidx;
+    }
+    // After a failed wait: wait (bounded) for the copies still in flight.
+    __device__ void drain()
+    {
+        for (; cidx != pidx; ++cidx) (void)mbar_wait(bar + cidx % NST, (cidx / NST) & 1u);
+    }
+};
+
+template <int CH, int NST, bool EVF>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_spmv_symb(SellView<float> U, const float *__restrict__ p, float *__restrict__ q4, KState *S, double *pd,
+                   float *pf, unsigned *ticket)
+{
+    extern __shared__ __align__(128) unsigned char dsm[];
+    if (S->done | S->need_update) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    SliceStager<CH, NST, EVF> sg;
+    sg.init(dsm, U, w0, nw);
+
+    Comp32 dot[1] = {Comp32{0.f, 0.f}};
+    bool ok = true;
+    for (int64_t s = w0; ok && s < U.ns; s += nw) {
+        const int64_t b0 = U.sptr[s];
+        const int w = (int)(U.sptr[s + 1] - b0);
+        if (w <= 0) continue;
+        const int64_t row = s * 32 + lane;
+        const bool live = row < U.nb;
+        float xi[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) xi[t] = live ? __ldg(p + 3 * row + t) : 0.f;
+        float acc[3] = {0.f, 0.f, 0.f}, dg[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < w; k += CH) {
+            const int *cs;
+            const float *vs;
+            if (!sg.wait(cs, vs)) {
+                ok = false;
+                break;
+            }
+            const int nsl = min(CH, w - k);
+            int c[CH];
+            float xj[CH][3];
+#pragma unroll
+            for (int j = 0; j < CH; ++j)
+                if (j < nsl) {
+                    c[j] = cs[j * 32 + lane];
+#pragma unroll
+                    for (int t = 0; t < 3; ++t) xj[j][t] = __ldg(p + 3 * (int64_t)c[j] + t);
+                }
+#pragma unroll
+            for (int j = 0; j < CH; ++j)
+                if (j < nsl) {
+                    float a[9];
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) a[e] = vs[(j * 9 + e) * 32 + lane];
+                    float bx[3];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+                        bx[r] = fmaf(a[3 * r], xj[j][0], fmaf(a[3 * r + 1], xj[j][1], a[3 * r + 2] * xj[j][2]));
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) acc[r] += bx[r];
+                    if (c[j] == row) {
+#pragma unroll
+                        for (int r = 0; r < 3; ++r) dg[r] += bx[r];
+                    } else if (live) {
+                        float tv[3];
+#pragma unroll
+                        for (int t = 0; t < 3; ++t) tv[t] = fmaf(a[t], xi[0], fmaf(a[3 + t], xi[1], a[6 + t] * xi[2]));
+                        red_add_v4(q4 + 4 * (int64_t)c[j], tv[0], tv[1], tv[2]);
+                    }
+                }
+            sg.release();
+        }
+        if (ok && live) {
+            red_add_v4(q4 + 4 * row, acc[0], acc[1], acc[2]);
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                comp_add_prod(dot[0], 2.f * xi[r], acc[r]);
+                comp_add_prod(dot[0], -xi[r], dg[r]);
+            }
+        }
+    }
+    if (!ok) {
+        if (lane == 0) {
+            S->status = PFG_E_INTERNAL;
+            S->done = 1;
+        }
+        sg.drain();
+    }
+    float tot[1];
+    if (grid_total<1>(dot, pd, pf, ticket, tot) && !S->done) {
+        const double pq = (double)tot[0];
+        if (!(pq > 0.0) || !finite_d(pq)) {
+            S->status = PFG_E_BREAKDOWN;
+            S->done = 1;
+        } else {
+            S->alpha32 = (float)(S->rho32 / tot[0]);
+        }
+    }
+}
+
+constexpr int kSymbSlots = 2, kSymbStages = 4;
+using SymbLayout = SymBulk<kSymbSlots, kSymbStages>;
+#define k_cg_spmv_sym k_cg_spmv_symb<kSymbSlots, kSymbStages, true>
+
+// Grid of a bulk-staged kernel: its resident CTAs with `smem` bytes of
+// dynamic shared memory each, capped by the slices.  The first call per
+// kernel raises the kernel's dynamic shared-memory limit, so it is made before
+// any graph capture.
+template <typename K>
+static int staged_grid(K kern, int smem, int64_t ns)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void *, int> cache;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find((const void *)kern);
+        if (it == cache.end()) {
+            PFG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+            cache[(const void *)kern] = per_sm;
+        } else {
+            per_sm = it->second;
+        }
+    }
+    const int64_t want = (ns + kWarps - 1) / kWarps;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(per_sm, 1) * sm_count()));
+}
+
+static void launch_cg_spmv_sym(const SellView<float> &U, const float *p, float *q4, KState *S, double *pd,
+                               float *pf, unsigned *tk, cudaStream_t st)
+{
+    k_cg_spmv_sym<<<staged_grid(k_cg_spmv_sym, SymbLayout::kSmem, U.ns), kThreads, SymbLayout::kSmem, st>>>(
+        U, p, q4, S, pd, pf, tk);
+}
 
 // Reproducible form of the symmetric product (the BiCGSTAB inner iterations,
 // whose iteration count follows every rounding difference).  Each row's own
@@ -1139,7 +1389,90 @@ __global__ void __launch_bounds__(kThreads, MINB)
 }
 // one slot per loop step at 5 CTAs per SM: 0.113 ms per launch at 3.09M DOF
 // (two slots at 4 CTAs: 0.127 ms)
-#define k_spmv_symfx k_spmv_symfx_t<1, 5>
+
+// The same product with the matrix planes staged in shared memory by bulk
+// copies (SliceStager, as k_cg_spmv_symb).  Each lane sums its row's own
+// blocks in slot order, as above, so the results are the same bits.
+template <int CH, int NST, bool EVF>
+__global__ void __launch_bounds__(kThreads)
+    k_spmv_symfxb(SellView<float> U, const float *__restrict__ x, float *__restrict__ y,
+                  unsigned long long *__restrict__ acc64, float rowsum, KState *S)
+{
+    extern __shared__ __align__(128) unsigned char dsm[];
+    if (S->done | S->need_update) return;
+    const float scale = exp2f((float)symfx_exponent(rowsum, S->xmax_bits));
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    SliceStager<CH, NST, EVF> sg;
+    sg.init(dsm, U, w0, nw);
+    bool ok = true;
+    for (int64_t s = w0; ok && s < U.ns; s += nw) {
+        const int64_t b0 = U.sptr[s];
+        const int w = (int)(U.sptr[s + 1] - b0);
+        if (w <= 0) continue;
+        const int64_t row = s * 32 + lane;
+        const bool live = row < U.nb;
+        float xi[3];
+#pragma unroll
+        for (int t = 0; t < 3; ++t) xi[t] = live ? __ldg(x + 3 * row + t) : 0.f;
+        float acc[3] = {0.f, 0.f, 0.f};
+        for (int k = 0; k < w; k += CH) {
+            const int *cs;
+            const float *vs;
+            if (!sg.wait(cs, vs)) {
+                ok = false;
+                break;
+            }
+            const int nsl = min(CH, w - k);
+            int c[CH];
+            float xj[CH][3];
+#pragma unroll
+            for (int j = 0; j < CH; ++j)
+                if (j < nsl) {
+                    c[j] = cs[j * 32 + lane];
+#pragma unroll
+                    for (int t = 0; t < 3; ++t) xj[j][t] = __ldg(x + 3 * (int64_t)c[j] + t);
+                }
+#pragma unroll
+            for (int j = 0; j < CH; ++j)
+                if (j < nsl) {
+                    float a[9];
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) a[e] = vs[(j * 9 + e) * 32 + lane];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+                        acc[r] += fmaf(a[3 * r], xj[j][0], fmaf(a[3 * r + 1], xj[j][1], a[3 * r + 2] * xj[j][2]));
+                    if (live && c[j] != row) {
+#pragma unroll
+                        for (int t = 0; t < 3; ++t) {
+                            const float tv = fmaf(a[t], xi[0], fmaf(a[3 + t], xi[1], a[6 + t] * xi[2]));
+                            red_add_u64(acc64 + (int64_t)t * U.nb + c[j], __float2ll_rn(tv * scale));
+                        }
+                    }
+                }
+            sg.release();
+        }
+        if (ok && live)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) y[3 * row + t] = acc[t];
+    }
+    if (!ok) {
+        if (lane == 0) {
+            S->status = PFG_E_INTERNAL;
+            S->done = 1;
+        }
+        sg.drain();
+    }
+}
+#define k_spmv_symfx k_spmv_symfxb<kSymbSlots, kSymbStages, true>
+
+static void launch_spmv_symfx(const SellView<float> &U, const float *x, float *y, unsigned long long *acc64,
+                              float rowsum, KState *S, cudaStream_t st)
+{
+    k_spmv_symfx<<<staged_grid(k_spmv_symfx, SymbLayout::kSmem, U.ns), kThreads, SymbLayout::kSmem, st>>>(
+        U, x, y, acc64, rowsum, S);
+}
 
 // y += acc64 / scale (acc64 = 0 for the next product), then the dot products
 // and scalar updates of the BiCGSTAB products:
@@ -1576,11 +1909,10 @@ static int cg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *
 {
     const int64_t n = nb * 3;
     const int gd = resident_grid(k_cg_dir<float>, (n + 31) / 32);
-    const int gs = resident_grid(k_cg_spmv_sym, U.ns);
     const int gu = resident_grid(k_cg_update<3, float, 4>, (nb + 31) / 32);
     for (int it = 0; it < chunk; ++it) {
         k_cg_dir<float><<<gd, kThreads, 0, st>>>(n, z, p, S);
-        k_cg_spmv_sym<<<gs, kThreads, 0, st>>>(U, p, q4, S, pd, pf, tk);
+        launch_cg_spmv_sym(U, p, q4, S, pd, pf, tk, st);
         k_cg_update<3, float, 4><<<gu, kThreads, 0, st>>>(nb, x, r, z, p, p, q4, dinv, pc, S, pd, pf, tk, tol,
                                                           delta, itrmax);
     }
@@ -1602,15 +1934,14 @@ static int bicg_chunk_sym(const SellView<float> &U, float rowsum, int chunk, int
     float *ehat = pc != PFG_PC_NONE ? eh : e;
     const int gd = resident_grid(k_bicg_dir<3, float>, (nb + 31) / 32);
     const int ge = resident_grid(k_bicg_e<3, float>, (nb + 31) / 32);
-    const int gs = resident_grid(k_spmv_symfx, U.ns);
     const int gf = resident_grid(k_symfx_finish, (3 * nb + 127) / 128);
     const int g3 = resident_grid(k_bicg_update<3, float>, nvec);
     for (int it = 0; it < chunk; ++it) {
         k_bicg_dir<3, float><<<gd, kThreads, 0, st>>>(nb, r, p, y, ph, dinv, pc, S, true);
-        k_spmv_symfx<<<gs, kThreads, 0, st>>>(U, phat, y, fx, rowsum, S);
+        launch_spmv_symfx(U, phat, y, fx, rowsum, S, st);
         k_symfx_finish<<<gf, kThreads, 0, st>>>(nb, y, fx, r0, rowsum, 1, S, pd, pf, tk);
         k_bicg_e<3, float><<<ge, kThreads, 0, st>>>(nb, r, y, e, eh, dinv, pc, S, true);
-        k_spmv_symfx<<<gs, kThreads, 0, st>>>(U, ehat, v, fx, rowsum, S);
+        launch_spmv_symfx(U, ehat, v, fx, rowsum, S, st);
         k_symfx_finish<<<gf, kThreads, 0, st>>>(nb, v, fx, e, rowsum, 2, S, pd, pf, tk);
         k_bicg_update<3, float><<<g3, kThreads, 0, st>>>(nb, x, r, r0, phat, phat, e, ehat, v, S, pd, pf, tk,
                                                          PFG_STOP_TRUE_RELATIVE, er0, tol, delta, itrmax);
@@ -1878,6 +2209,8 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
             PFG_CUDA(cudaMemsetAsync(fx_.p, 0, (size_t)A.nb * 3 * sizeof(unsigned long long), st));
         }
     }
+    if (sym)  // (the first call per kernel sets a kernel attribute: outside capture)
+        cg ? staged_grid(k_cg_spmv_sym, SymbLayout::kSmem, A.ns_u) : staged_grid(k_spmv_symfx, SymbLayout::kSmem, A.ns_u);
     const uint64_t key = graph_key(cg ? 3 : 4, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -2096,7 +2429,7 @@ __global__ void k_fill(double *a, int64_t n, double v)
 
 void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double &ms, double &bytes)
 {
-    PFG_CHECK(kernel >= 0 && kernel <= 10 && reps > 0, PFG_E_ARG, "bad profile request");
+    PFG_CHECK(kernel >= 0 && kernel <= 12 && reps > 0, PFG_E_ARG, "bad profile request");
     if (kernel == 9) {
         // one D^-1 L^-1 sweep of the held ILU(0) factor (factored in
         // ascending column order if none is held)
@@ -2134,7 +2467,7 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
         y4_.ensure((size_t)A.nb * 4);
         PFG_CUDA(cudaMemsetAsync(y4_.p, 0, (size_t)A.nb * 4 * sizeof(float), st));
     }
-    if (kernel == 10) {
+    if (kernel == 10 || kernel == 12) {
         fx_.ensure((size_t)A.nb * 3);
         PFG_CUDA(cudaMemsetAsync(fx_.p, 0, (size_t)A.nb * 3 * sizeof(unsigned long long), st));
     }
@@ -2199,12 +2532,18 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
                                                                               nullptr);
             break;
         case 8:
-            k_cg_spmv_sym<<<resident_grid(k_cg_spmv_sym, A.ns_u), kThreads, 0, st>>>(
+            launch_cg_spmv_sym(sell_upper(A), x32.p, y4_.p, state_.p, partials_.p, partials32_.p, ticket_.p, st);
+            break;
+        case 11:
+            k_cg_spmv_sym_t<2, 4><<<resident_grid(k_cg_spmv_sym_t<2, 4>, A.ns_u), kThreads, 0, st>>>(
                 sell_upper(A), x32.p, y4_.p, state_.p, partials_.p, partials32_.p, ticket_.p);
             break;
         case 10:  // (its finish pass, which adds and clears the transposes, is not part of the launch)
-            k_spmv_symfx<<<resident_grid(k_spmv_symfx, A.ns_u), kThreads, 0, st>>>(sell_upper(A), x32.p, y32.p,
-                                                                                  fx_.p, A.sym_rowsum, state_.p);
+            launch_spmv_symfx(sell_upper(A), x32.p, y32.p, fx_.p, A.sym_rowsum, state_.p, st);
+            break;
+        case 12:
+            k_spmv_symfx_t<1, 5><<<resident_grid(k_spmv_symfx_t<1, 5>, A.ns_u), kThreads, 0, st>>>(
+                sell_upper(A), x32.p, y32.p, fx_.p, A.sym_rowsum, state_.p);
             break;
         case 3:
             if (A.bs == 3) k_spmv<3, double><<<gb, kThreads, 0, st>>>(A.view<double>(), x64.p, y64.p);
@@ -2250,7 +2589,7 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     ms = (double)t / reps;
-    if (kernel == 2 || kernel == 5 || kernel == 6 || kernel == 8) {
+    if (kernel == 2 || kernel == 5 || kernel == 6 || kernel == 8 || kernel == 11) {
         KState h;
         read_state(h, st);
         PFG_CHECK(!h.done, PFG_E_BREAKDOWN, "profiled CG SpMV hit p.Ap <= 0 (matrix not positive definite)");

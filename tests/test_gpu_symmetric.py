@@ -79,18 +79,19 @@ def test_symmetric_storage_larger_mesh_twice(cuda):
 
 def test_symmetric_product_profiles(cuda):
     """The profiled symmetric product runs and reports half the matrix bytes
-    of the full product (kernels 7, 8 of pfg_profile_kernel)."""
+    of the full product (kernels 7, 8 of pfg_profile_kernel; 11 is 8 without
+    the shared-memory staging)."""
     p, _ = _system(8)
     s = _solver(p)
     s.eliminate()
     lib = N.load()
     got = {}
-    for kid in (1, 7, 8):
+    for kid in (1, 7, 8, 11):
         ms, by = C.c_double(), C.c_double()
         N.check(lib.pfg_profile_kernel(s.handle, kid, 3, C.byref(ms), C.byref(by)))
         got[kid] = by.value
         assert ms.value > 0.0
-    assert got[7] == got[8] and 0.45 * got[1] < got[7] < 0.65 * got[1]
+    assert got[7] == got[8] == got[11] and 0.45 * got[1] < got[7] < 0.65 * got[1]
 
 
 @pytest.mark.parametrize("pc", ["BlockJacobi", None])
