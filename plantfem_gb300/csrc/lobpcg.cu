@@ -259,6 +259,80 @@ __device__ __forceinline__ const T *panel_row(const T *base, int64_t n, int q, i
     return base + ((int64_t)q * n + row) * PW;
 }
 
+// A panel row (PW = 8 consecutive values, 32 or 64 bytes, aligned to its
+// size) moved with 16-byte accesses: one gather instruction per 16 bytes
+// instead of one per value.
+__device__ __forceinline__ void ld_row(const float *p, float (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const float4 w = __ldg(reinterpret_cast<const float4 *>(p) + u);
+        v[4 * u] = w.x;
+        v[4 * u + 1] = w.y;
+        v[4 * u + 2] = w.z;
+        v[4 * u + 3] = w.w;
+    }
+}
+__device__ __forceinline__ void ld_row(const double *p, double (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const double2 w = __ldg(reinterpret_cast<const double2 *>(p) + u);
+        v[2 * u] = w.x;
+        v[2 * u + 1] = w.y;
+    }
+}
+__device__ __forceinline__ void ld_row(const float2 *p, float2 (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const float4 w = __ldg(reinterpret_cast<const float4 *>(p) + u);
+        v[2 * u] = make_float2(w.x, w.y);
+        v[2 * u + 1] = make_float2(w.z, w.w);
+    }
+}
+__device__ __forceinline__ void st_row(float *p, const float (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+        reinterpret_cast<float4 *>(p)[u] = make_float4(v[4 * u], v[4 * u + 1], v[4 * u + 2], v[4 * u + 3]);
+}
+__device__ __forceinline__ void st_row(double *p, const double (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u) reinterpret_cast<double2 *>(p)[u] = make_double2(v[2 * u], v[2 * u + 1]);
+}
+// The same from shared memory (plain loads: __ldg is for global memory).
+__device__ __forceinline__ void lds_row(const float *p, float (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const float4 w = reinterpret_cast<const float4 *>(p)[u];
+        v[4 * u] = w.x;
+        v[4 * u + 1] = w.y;
+        v[4 * u + 2] = w.z;
+        v[4 * u + 3] = w.w;
+    }
+}
+__device__ __forceinline__ void lds_row(const double *p, double (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const double2 w = reinterpret_cast<const double2 *>(p)[u];
+        v[2 * u] = w.x;
+        v[2 * u + 1] = w.y;
+    }
+}
+__device__ __forceinline__ void lds_row(const float2 *p, float2 (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const float4 w = reinterpret_cast<const float4 *>(p)[u];
+        v[2 * u] = make_float2(w.x, w.y);
+        v[2 * u + 1] = make_float2(w.z, w.w);
+    }
+}
+
 // Double-FP32 ("double-float") arithmetic on the FP32 pipe, for the second
 // phase of the mixed LOBPCG (its Gram, SpMM and linear combinations of FP64
 // panels): GB300's FP64 pipe is about 1/30 of its FP32 pipe, and the FP64
@@ -323,10 +397,8 @@ __global__ void __launch_bounds__(kT) k_spmm(SellView<T> A, int np, const T *__r
             for (int e = 0; e < BS * BS; ++e) a[e] = ld_stream(vp + ((int64_t)k * (BS * BS) + e) * 32);
 #pragma unroll
             for (int cc = 0; cc < BS; ++cc) {
-                const T *xr = panel_row(X, n, q, (int64_t)BS * col + cc);
                 T xv[PW];
-#pragma unroll
-                for (int c = 0; c < PW; ++c) xv[c] = __ldg(xr + c);
+                ld_row(panel_row(X, n, q, (int64_t)BS * col + cc), xv);
 #pragma unroll
                 for (int r = 0; r < BS; ++r)
 #pragma unroll
@@ -338,10 +410,10 @@ __global__ void __launch_bounds__(kT) k_spmm(SellView<T> A, int np, const T *__r
 #pragma unroll
             for (int r = 0; r < BS; ++r) {
                 const int64_t i = (int64_t)BS * row + r;
-                const bool f = fixed && fixed[i];
-                T *yr = Y + ((int64_t)q * n + i) * PW;
+                if (fixed && fixed[i])
 #pragma unroll
-                for (int c = 0; c < PW; ++c) yr[c] = f ? T(0) : acc[r][c];
+                    for (int c = 0; c < PW; ++c) acc[r][c] = T(0);
+                st_row(Y + ((int64_t)q * n + i) * PW, acc[r]);
             }
         }
     }
@@ -388,10 +460,8 @@ __global__ void __launch_bounds__(kT) k_spmm_df(SellView<double> A, const float2
             for (int e = 0; e < BS * BS; ++e) a[e] = __ldg(vp + ((int64_t)k * (BS * BS) + e) * 32);
 #pragma unroll
             for (int cc = 0; cc < BS; ++cc) {
-                const float2 *xr = panel_row(X, n, q, (int64_t)BS * col + cc);
                 float2 xv[PW];
-#pragma unroll
-                for (int c = 0; c < PW; ++c) xv[c] = __ldg(xr + c);
+                ld_row(panel_row(X, n, q, (int64_t)BS * col + cc), xv);
 #pragma unroll
                 for (int r = 0; r < BS; ++r)
 #pragma unroll
@@ -404,9 +474,10 @@ __global__ void __launch_bounds__(kT) k_spmm_df(SellView<double> A, const float2
             for (int r = 0; r < BS; ++r) {
                 const int64_t i = (int64_t)BS * row + r;
                 const bool f = fixed && fixed[i];
-                double *yr = Y + ((int64_t)q * n + i) * PW;
+                double yv[PW];
 #pragma unroll
-                for (int c = 0; c < PW; ++c) yr[c] = f ? 0.0 : acc[r][c].get();
+                for (int c = 0; c < PW; ++c) yv[c] = f ? 0.0 : acc[r][c].get();
+                st_row(Y + ((int64_t)q * n + i) * PW, yv);
             }
         }
     }
@@ -418,13 +489,16 @@ __global__ void __launch_bounds__(kT)
                  const float2 *__restrict__ P, const double *__restrict__ C, double *__restrict__ Xn,
                  double *__restrict__ Pn)
 {
-    extern __shared__ unsigned char smraw[];
+    extern __shared__ __align__(16) unsigned char smraw[];
     float2 *sC = (float2 *)smraw;
     const int m = nblk * k;
     const int np = (k + PW - 1) / PW;
-    for (int i = threadIdx.x; i < m * k; i += blockDim.x) sC[i] = df_split(C[i]);
+    const int kp = np * PW;
+    for (int e = threadIdx.x; e < m * kp; e += blockDim.x) {
+        const int r = e / kp, j = e - r * kp;
+        sC[e] = j < k ? df_split(C[(int64_t)j * m + r]) : make_float2(0.f, 0.f);
+    }
     __syncthreads();
-    const float2 *B[3] = {X, W, P};
     for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
         for (int qo = 0; qo < np; ++qo) {
             DFAcc ax[PW], ap[PW];
@@ -435,35 +509,32 @@ __global__ void __launch_bounds__(kT)
             }
             for (int b = 0; b < nblk; ++b) {
                 for (int qi = 0; qi < np; ++qi) {
-                    const float2 *src = panel_row(B[b], n, qi, row);
                     float2 v[PW];
-#pragma unroll
-                    for (int c = 0; c < PW; ++c) v[c] = src[c];
+                    ld_row(panel_row(b == 0 ? X : (b == 1 ? W : P), n, qi, row), v);
 #pragma unroll
                     for (int c = 0; c < PW; ++c) {
                         const int i = qi * PW + c;
                         if (i >= k) break;
-                        const float2 *crow = sC + (b * k + i);
+                        float2 cr[PW];
+                        lds_row(sC + (int64_t)(b * k + i) * kp + qo * PW, cr);
 #pragma unroll
                         for (int o = 0; o < PW; ++o) {
-                            const int jj = qo * PW + o;
-                            const float2 cij = jj < k ? crow[(int64_t)jj * m] : make_float2(0.f, 0.f);
                             if (b == 0)
-                                ax[o].add(v[c], cij);
+                                ax[o].add(v[c], cr[o]);
                             else
-                                ap[o].add(v[c], cij);
+                                ap[o].add(v[c], cr[o]);
                         }
                     }
                 }
             }
-            double *xo = Xn + ((int64_t)qo * n + row) * PW;
-            double *po = Pn + ((int64_t)qo * n + row) * PW;
+            double pv[PW], xv[PW];
 #pragma unroll
             for (int o = 0; o < PW; ++o) {
-                const double pv = ap[o].get();
-                po[o] = pv;
-                xo[o] = ax[o].get() + pv;
+                pv[o] = ap[o].get();
+                xv[o] = ax[o].get() + pv[o];
             }
+            st_row(Pn + ((int64_t)qo * n + row) * PW, pv);
+            st_row(Xn + ((int64_t)qo * n + row) * PW, xv);
         }
     }
 }
@@ -523,6 +594,58 @@ struct GramArith<double, true> {
 constexpr int kGramRows = 32;  // rows staged in shared memory per step
 constexpr int kGramSub = 4;    // each thread owns a 4 x 4 sub-tile of both Gram matrices
 
+// Shared-memory tile of the Gram staging: kGramRows rows of one 8-column
+// panel, row-major, followed by 64 bytes of padding so that consecutive tiles
+// start 16 banks apart (the 16-byte loads of the threads of a quarter warp,
+// which read two neighbouring tiles, then hit distinct banks).
+template <typename St>
+__host__ __device__ constexpr int gram_tile_elems()
+{
+    return kGramRows * PW + 64 / (int)sizeof(St);
+}
+
+// 16-byte moves of staged values: global (T) -> shared (St), 16 bytes of
+// source per call.
+__device__ __forceinline__ void gram_stage16(const float *src, float *dst)
+{
+    *reinterpret_cast<float4 *>(dst) = __ldg(reinterpret_cast<const float4 *>(src));
+}
+__device__ __forceinline__ void gram_stage16(const double *src, double *dst)
+{
+    *reinterpret_cast<double2 *>(dst) = __ldg(reinterpret_cast<const double2 *>(src));
+}
+__device__ __forceinline__ void gram_stage16(const double *src, float2 *dst)  // split into double-float
+{
+    const double2 w = __ldg(reinterpret_cast<const double2 *>(src));
+    const float2 a = df_split(w.x), b = df_split(w.y);
+    *reinterpret_cast<float4 *>(dst) = make_float4(a.x, a.y, b.x, b.y);
+}
+// four consecutive staged values (16- or 32-byte aligned)
+__device__ __forceinline__ void gram_lds4(const float *p, float (&v)[kGramSub])
+{
+    const float4 w = *reinterpret_cast<const float4 *>(p);
+    v[0] = w.x;
+    v[1] = w.y;
+    v[2] = w.z;
+    v[3] = w.w;
+}
+__device__ __forceinline__ void gram_lds4(const double *p, double (&v)[kGramSub])
+{
+    const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+}
+__device__ __forceinline__ void gram_lds4(const float2 *p, float2 (&v)[kGramSub])
+{
+    const float4 a = reinterpret_cast<const float4 *>(p)[0], b = reinterpret_cast<const float4 *>(p)[1];
+    v[0] = make_float2(a.x, a.y);
+    v[1] = make_float2(a.z, a.w);
+    v[2] = make_float2(b.x, b.y);
+    v[3] = make_float2(b.z, b.w);
+}
+
 // Upper triangles of S^T (K S) and S^T (M S), S = [X W P] (nblk blocks of k
 // columns, each padded to kp = 8 np columns): each CTA reduces a contiguous
 // row range and writes its partial sums (FP64) to part[cta][2 * npairs], pair
@@ -532,18 +655,24 @@ constexpr int kGramSub = 4;    // each thread owns a 4 x 4 sub-tile of both Gram
 // Register-tiled outer products: the padded m_p x m_p matrix is cut into 8 x 8
 // tiles; the upper-triangle tiles (I <= J) are split into four 4 x 4 sub-tiles,
 // one per thread (4 * T (T + 1) / 2 threads for T = m_p / 8 tile columns, at
-// most 312).  Per staged row a thread reads 4 values of S and 4 of each image
-// and does 32 multiply-adds: compensated FP32 for FP32 panels, FP64 for FP64
-// panels, or double-float (DF, the mixed mode's second phase) on the FP32
-// pipe, the operands split once when a row is staged.  The sub-tile below the diagonal of a diagonal tile is
-// computed and not written.
+// most 312).  A step stages kGramRows rows of every panel of S, K S and M S
+// into shared memory, one panel tile after another: the rows of a panel are
+// contiguous in global memory, so each warp copies whole tiles with 16-byte
+// loads.  Per staged row a thread reads its 4 values of S and 4 of each image
+// with 16-byte shared loads and does 32 multiply-adds: FP32 for FP32 panels
+// (per CTA row range; the ranges are summed in FP64), FP64 for FP64 panels,
+// or double-float (DF, the mixed mode's second phase) on the FP32 pipe, the
+// operands split once when staged.  Padding columns are staged as they are
+// stored and their sums are not written; the sub-tile below the diagonal of
+// a diagonal tile is computed and not written.
 template <typename T, bool DF>
 __global__ void __launch_bounds__(320)
     k_gram(int64_t n, int k, int nblk, const T *S0, const T *S1, const T *S2, const T *K0, const T *K1, const T *K2,
            const T *M0, const T *M1, const T *M2, double *part)
 {
-    extern __shared__ unsigned char smraw[];
+    extern __shared__ __align__(16) unsigned char smraw[];
     const int kp = (k + PW - 1) / PW * PW;
+    const int np = kp / PW;
     const int mp = nblk * kp;
     const int m = nblk * k;
     const int npairs = m * (m + 1) / 2;
@@ -551,11 +680,10 @@ __global__ void __launch_bounds__(320)
     const int ntasks = kGramSub * tiles * (tiles + 1) / 2;
     using Ar = GramArith<T, DF>;
     using St = typename Ar::Stage;
-    St *sS = (St *)smraw;
-    St *sK = sS + kGramRows * mp;
-    St *sM = sK + kGramRows * mp;
+    constexpr int TE = gram_tile_elems<St>();
+    St *sS = (St *)smraw;  // [3][tiles][TE]: S, K S, M S
     const bool active = (int)threadIdx.x < ntasks;
-    int i0 = 0, j0 = 0;
+    int ti = 0, tj = 0, oi = 0, oj = 0;
     if (active) {
         const int tp = threadIdx.x >> 2, sub = threadIdx.x & 3;
         int I = 0, rem = tp;
@@ -563,8 +691,10 @@ __global__ void __launch_bounds__(320)
             rem -= tiles - I;
             ++I;
         }
-        i0 = PW * I + kGramSub * (sub >> 1);
-        j0 = PW * (I + rem) + kGramSub * (sub & 1);
+        ti = I;
+        tj = I + rem;
+        oi = kGramSub * (sub >> 1);
+        oj = kGramSub * (sub & 1);
     }
     typename Ar::Acc aA[kGramSub][kGramSub], aB[kGramSub][kGramSub];
 #pragma unroll
@@ -576,31 +706,29 @@ __global__ void __launch_bounds__(320)
         }
     const int64_t per = (n + gridDim.x - 1) / gridDim.x;
     const int64_t r0 = (int64_t)blockIdx.x * per, r1 = min(n, r0 + per);
-    const T *SS[3] = {S0, S1, S2}, *KK[3] = {K0, K1, K2}, *MM[3] = {M0, M1, M2};
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    constexpr int kPer16 = 16 / (int)sizeof(T);  // source values per 16-byte move
+    const St *pS = sS + ti * TE + oi, *pK = sS + (tiles + tj) * TE + oj, *pM = sS + (2 * tiles + tj) * TE + oj;
     for (int64_t t0 = r0; t0 < r1; t0 += kGramRows) {
         const int rows = (int)((r1 - t0) < (int64_t)kGramRows ? (r1 - t0) : (int64_t)kGramRows);
+        const int units = rows * PW / kPer16;  // 16-byte moves per tile
         __syncthreads();
-        // stage rows t0 .. t0+rows of every padded column; padding columns read as 0
-        for (int e = threadIdx.x; e < rows * mp; e += blockDim.x) {
-            const int r = e / mp, col = e - r * mp;
-            const int b = col / kp, cc = col - b * kp;
-            const int q = cc / PW, c = cc - q * PW;
-            const int64_t off = ((int64_t)q * n + t0 + r) * PW + c;
-            const bool real = cc < k;
-            sS[r * mp + col] = real ? Ar::stage(SS[b][off]) : Ar::none();
-            sK[r * mp + col] = real ? Ar::stage(KK[b][off]) : Ar::none();
-            sM[r * mp + col] = real ? Ar::stage(MM[b][off]) : Ar::none();
+        for (int ta = wid; ta < 3 * tiles; ta += nwarps) {
+            const int mat = ta / tiles, t = ta - mat * tiles;
+            const int b = t / np, q = t - b * np;
+            const T *base = mat == 0 ? (b == 0 ? S0 : (b == 1 ? S1 : S2))
+                                     : (mat == 1 ? (b == 0 ? K0 : (b == 1 ? K1 : K2)) : (b == 0 ? M0 : (b == 1 ? M1 : M2)));
+            const T *src = base + ((int64_t)q * n + t0) * PW;
+            St *dst = sS + ta * TE;
+            for (int u = lane; u < units; u += 32) gram_stage16(src + u * kPer16, dst + u * kPer16);
         }
         __syncthreads();
         if (active) {
             for (int r = 0; r < rows; ++r) {
                 St si[kGramSub], yk[kGramSub], ym[kGramSub];
-#pragma unroll
-                for (int a = 0; a < kGramSub; ++a) {
-                    si[a] = sS[r * mp + i0 + a];
-                    yk[a] = sK[r * mp + j0 + a];
-                    ym[a] = sM[r * mp + j0 + a];
-                }
+                gram_lds4(pS + r * PW, si);
+                gram_lds4(pK + r * PW, yk);
+                gram_lds4(pM + r * PW, ym);
 #pragma unroll
                 for (int a = 0; a < kGramSub; ++a)
 #pragma unroll
@@ -616,7 +744,7 @@ __global__ void __launch_bounds__(320)
     for (int a = 0; a < kGramSub; ++a)
 #pragma unroll
         for (int b = 0; b < kGramSub; ++b) {
-            const int pi = i0 + a, pj = j0 + b;  // padded columns
+            const int pi = PW * ti + oi + a, pj = PW * tj + oj + b;  // padded columns
             const int bi = pi / kp, ci = pi - bi * kp, bj = pj / kp, cj = pj - bj * kp;
             if (ci >= k || cj >= k) continue;
             const int i = bi * k + ci, j = bj * k + cj;
@@ -637,19 +765,27 @@ __global__ void k_reduce_parts(const double *__restrict__ part, int nparts, int 
     }
 }
 
-// Pn = W C_w + P C_p ; Xn = X C_x + Pn   (C: m x k column-major, FP64)
+// Pn = W C_w + P C_p ; Xn = X C_x + Pn   (C: m x k column-major, FP64).
+// A thread per row and output panel.  The coefficients are staged transposed,
+// sC[(b k + i) kp + j] with j padded to kp by zeros, so the 8 coefficients of
+// one input value for one output panel are a 16-byte-aligned row of shared
+// memory (2 or 4 vector loads per 8 multiply-adds); the input and output rows
+// move with 16-byte accesses.
 template <typename T>
 __global__ void __launch_bounds__(kT)
     k_lincomb(int64_t n, int k, int nblk, const T *__restrict__ X, const T *__restrict__ W, const T *__restrict__ P,
               const double *__restrict__ C, T *__restrict__ Xn, T *__restrict__ Pn)
 {
-    extern __shared__ unsigned char smraw[];
+    extern __shared__ __align__(16) unsigned char smraw[];
     T *sC = (T *)smraw;
     const int m = nblk * k;
     const int np = (k + PW - 1) / PW;
-    for (int i = threadIdx.x; i < m * k; i += blockDim.x) sC[i] = (T)C[i];
+    const int kp = np * PW;
+    for (int e = threadIdx.x; e < m * kp; e += blockDim.x) {
+        const int r = e / kp, j = e - r * kp;
+        sC[e] = j < k ? (T)C[(int64_t)j * m + r] : T(0);
+    }
     __syncthreads();
-    const T *B[3] = {X, W, P};
     for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
         for (int qo = 0; qo < np; ++qo) {
             T ax[PW], ap[PW];
@@ -657,84 +793,88 @@ __global__ void __launch_bounds__(kT)
             for (int c = 0; c < PW; ++c) ax[c] = ap[c] = T(0);
             for (int b = 0; b < nblk; ++b) {
                 for (int qi = 0; qi < np; ++qi) {
-                    const T *src = panel_row(B[b], n, qi, row);
                     T v[PW];
-#pragma unroll
-                    for (int c = 0; c < PW; ++c) v[c] = src[c];
+                    ld_row(panel_row(b == 0 ? X : (b == 1 ? W : P), n, qi, row), v);
 #pragma unroll
                     for (int c = 0; c < PW; ++c) {
                         const int i = qi * PW + c;
                         if (i >= k) break;
-                        const T *crow = sC + (b * k + i);  // C[(b k + i), j] at crow[j * m]
+                        T cr[PW];
+                        lds_row(sC + (int64_t)(b * k + i) * kp + qo * PW, cr);
 #pragma unroll
                         for (int o = 0; o < PW; ++o) {
-                            const int j = qo * PW + o;
-                            const T cij = j < k ? crow[(int64_t)j * m] : T(0);
                             if (b == 0)
-                                ax[o] = fma(v[c], cij, ax[o]);
+                                ax[o] = fma(v[c], cr[o], ax[o]);
                             else
-                                ap[o] = fma(v[c], cij, ap[o]);
+                                ap[o] = fma(v[c], cr[o], ap[o]);
                         }
                     }
                 }
             }
-            T *xo = Xn + ((int64_t)qo * n + row) * PW;
-            T *po = Pn + ((int64_t)qo * n + row) * PW;
 #pragma unroll
-            for (int o = 0; o < PW; ++o) {
-                po[o] = ap[o];
-                xo[o] = ax[o] + ap[o];
-            }
+            for (int o = 0; o < PW; ++o) ax[o] += ap[o];
+            st_row(Pn + ((int64_t)qo * n + row) * PW, ap);
+            st_row(Xn + ((int64_t)qo * n + row) * PW, ax);
         }
     }
 }
 
 // R = KX - MX diag(lam); per column: |R_j|^2, |MX_j|^2, max|R_j|  -> part[cta][3k]
+// (entry 3 j + {0, 1, 2} of CTA x's row).  CTA (x, q) takes the rows of panel
+// q, so a thread's sums are 3 x 8 registers and its rows move as vectors.
 template <typename T>
 __global__ void __launch_bounds__(kT)
     k_residual(int64_t n, int k, const T *__restrict__ KX, const T *__restrict__ MX, const double *__restrict__ lam,
                T *__restrict__ R, double *part)
 {
-    __shared__ double sred[3 * 32][kT / 32];
-    const int np = (k + PW - 1) / PW;
-    double rr[32], mm[32], mx[32];
-    for (int j = 0; j < 32; ++j) rr[j] = mm[j] = mx[j] = 0.0;
-    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
-        for (int q = 0; q < np; ++q) {
-            const int64_t off = ((int64_t)q * n + row) * PW;
+    __shared__ double sred[3 * PW][kT / 32];
+    const int q = blockIdx.y;
+    double rr[PW], mm[PW], mx[PW];
+    T lq[PW];
 #pragma unroll
-            for (int c = 0; c < PW; ++c) {
-                const int j = q * PW + c;
-                if (j >= k) {
-                    R[off + c] = T(0);
-                    continue;
-                }
-                const T mxv = MX[off + c];
-                const T r = KX[off + c] - mxv * (T)lam[j];
-                R[off + c] = r;
-                rr[j] += (double)r * (double)r;
-                mm[j] += (double)mxv * (double)mxv;
-                mx[j] = fmax(mx[j], fabs((double)r));
+    for (int c = 0; c < PW; ++c) {
+        rr[c] = mm[c] = mx[c] = 0.0;
+        lq[c] = q * PW + c < k ? (T)lam[q * PW + c] : T(0);
+    }
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t off = ((int64_t)q * n + row) * PW;
+        T kv[PW], mv[PW];
+        ld_row(KX + off, kv);
+        ld_row(MX + off, mv);
+#pragma unroll
+        for (int c = 0; c < PW; ++c) {
+            if (q * PW + c >= k) {
+                kv[c] = T(0);
+                continue;
             }
+            const T r = kv[c] - mv[c] * lq[c];
+            kv[c] = r;
+            rr[c] += (double)r * (double)r;
+            mm[c] += (double)mv[c] * (double)mv[c];
+            mx[c] = fmax(mx[c], fabs((double)r));
         }
+        st_row(R + off, kv);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int j = 0; j < k; ++j) {
-        double a = warp_sum(rr[j]), b = warp_sum(mm[j]), c = mx[j];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+    for (int c = 0; c < PW; ++c) {
+        double a = warp_sum(rr[c]), b = warp_sum(mm[c]), m = mx[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (lane == 0) {
-            sred[3 * j][wid] = a;
-            sred[3 * j + 1][wid] = b;
-            sred[3 * j + 2][wid] = c;
+            sred[3 * c][wid] = a;
+            sred[3 * c + 1][wid] = b;
+            sred[3 * c + 2][wid] = m;
         }
     }
     __syncthreads();
-    if (threadIdx.x < 3 * k) {
-        const int j = threadIdx.x / 3, t = threadIdx.x % 3;
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); ++w) s = t == 2 ? fmax(s, sred[3 * j + t][w]) : s + sred[3 * j + t][w];
-        part[(int64_t)blockIdx.x * 3 * k + threadIdx.x] = s;
+    if (threadIdx.x < 3 * PW) {
+        const int c = threadIdx.x / 3, t = threadIdx.x % 3;
+        if (q * PW + c < k) {
+            double v = 0.0;
+            for (int w = 0; w < (int)(blockDim.x / 32); ++w) v = t == 2 ? fmax(v, sred[3 * c + t][w]) : v + sred[3 * c + t][w];
+            part[(int64_t)blockIdx.x * 3 * k + 3 * (q * PW + c) + t] = v;
+        }
     }
 }
 
@@ -754,20 +894,21 @@ __global__ void __launch_bounds__(kT)
         for (int e = 0; e < BS * BS; ++e)
             D[e] = pc == PFG_PC_NONE ? (e % (BS + 1) == 0 ? 1.0 : 0.0) : dinv[node * BS * BS + e];
         for (int q = 0; q < np; ++q) {
-            const T *r0 = panel_row(R, n, q, (int64_t)BS * node);
-            T *w0 = W + ((int64_t)q * n + (int64_t)BS * node) * PW;
+            T rv[BS][PW];
 #pragma unroll
-            for (int c = 0; c < PW; ++c) {
-                double rv[BS];
+            for (int i = 0; i < BS; ++i) ld_row(panel_row(R, n, q, (int64_t)BS * node + i), rv[i]);
 #pragma unroll
-                for (int i = 0; i < BS; ++i) rv[i] = r0[i * PW + c];
+            for (int i = 0; i < BS; ++i) {
+                const bool f = fixed && fixed[(int64_t)BS * node + i];
+                T wv[PW];
 #pragma unroll
-                for (int i = 0; i < BS; ++i) {
+                for (int c = 0; c < PW; ++c) {
                     double v = 0.0;
 #pragma unroll
-                    for (int j = 0; j < BS; ++j) v += D[BS * i + j] * rv[j];
-                    w0[i * PW + c] = (fixed && fixed[(int64_t)BS * node + i]) ? T(0) : (T)v;
+                    for (int j = 0; j < BS; ++j) v += D[BS * i + j] * (double)rv[j][c];
+                    wv[c] = f ? T(0) : (T)v;
                 }
+                st_row(W + ((int64_t)q * n + (int64_t)BS * node + i) * PW, wv);
             }
         }
     }
@@ -945,7 +1086,8 @@ void gram(Ctx &c, int nblk, const Blocks<T> &B, std::vector<double> &GA, std::ve
     const int mp = nblk * c.kp;
     const int tiles = mp / PW;
     const int threads = (kGramSub * tiles * (tiles + 1) / 2 + 31) / 32 * 32;
-    const size_t smem = (size_t)3 * kGramRows * mp * sizeof(T);  // (a double-float operand is 8 bytes too)
+    // staged tiles: 3 matrices x tiles; a double-float value is 8 bytes like a double
+    const size_t smem = (size_t)3 * tiles * (kGramRows * PW + 64 / sizeof(T)) * sizeof(T);
     const int g = c.ngrid;
     c.part.ensure((size_t)g * 2 * npairs);
     c.gram.ensure((size_t)2 * npairs);
@@ -973,7 +1115,7 @@ template <typename T>
 void lincomb(Ctx &c, int nblk, const T *X, const T *W, const T *P, T *Xn, T *Pn)
 {
     const int m = nblk * c.k;
-    const size_t smem = (size_t)m * c.k * sizeof(T);
+    const size_t smem = (size_t)m * c.kp * sizeof(T);  // (a double-float coefficient is 8 bytes too)
     if constexpr (std::is_same<T, double>::value) {
         if (c.df) {  // float2 coefficients: the same 8 bytes each
             const int64_t len = c.n * c.kp;
@@ -1035,7 +1177,7 @@ ResInfo residuals(Ctx &c, Blocks<T> &B)
 {
     const int g = std::min(c.ngrid, 1024);
     c.part.ensure((size_t)g * 3 * c.k);
-    k_residual<T><<<g, kT, 0, c.st>>>(c.n, c.k, B.KX.p, B.MX.p, c.lam_d.p, B.R.p, c.part.p);
+    k_residual<T><<<dim3(g, c.np), kT, 0, c.st>>>(c.n, c.k, B.KX.p, B.MX.p, c.lam_d.p, B.R.p, c.part.p);
     PFG_CUDA(cudaGetLastError());
     ++c.launches;
     std::vector<double> h((size_t)g * 3 * c.k);
