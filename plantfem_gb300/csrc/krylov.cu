@@ -1183,13 +1183,23 @@ struct SliceStager {
     }
 };
 
-template <int CH, int NST, bool EVF>
+// FUSE: the direction update p = z + beta p rides in the product (as
+// k_cg_spmv does for the full copy): p_old is pA or pB by S->parity, every
+// gather forms z_j + beta p_old,j (the same FP32 fma as k_cg_dir, so the same
+// bits) and the lane that owns a row stores its p_new in the other buffer;
+// without FUSE, p = pA and z, pB are unused.
+template <int CH, int NST, bool EVF, bool FUSE>
 __global__ void __launch_bounds__(kThreads)
-    k_cg_spmv_symb(SellView<float> U, const float *__restrict__ p, float *__restrict__ q4, KState *S, double *pd,
-                   float *pf, unsigned *ticket)
+    k_cg_spmv_symb(SellView<float> U, const float *__restrict__ z, const float *pA, float *pB,
+                   float *__restrict__ q4, KState *S, double *pd, float *pf, unsigned *ticket)
 {
     extern __shared__ __align__(128) unsigned char dsm[];
     if (S->done | S->need_update) return;
+    const float beta = FUSE ? S->beta32 : 0.f;
+    const int par = FUSE ? S->parity : 0;
+    const float *p = (FUSE && par) ? pB : pA;                    // p (FUSE: p_old)
+    float *pnew = FUSE ? (par ? const_cast<float *>(pA) : pB) : nullptr;
+    auto pval = [&](int64_t i) { return FUSE ? fmaf(beta, __ldg(p + i), __ldg(z + i)) : __ldg(p + i); };
     const int lane = threadIdx.x & 31;
     const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -1206,7 +1216,10 @@ __global__ void __launch_bounds__(kThreads)
         const bool live = row < U.nb;
         float xi[3];
 #pragma unroll
-        for (int t = 0; t < 3; ++t) xi[t] = live ? __ldg(p + 3 * row + t) : 0.f;
+        for (int t = 0; t < 3; ++t) xi[t] = live ? pval(3 * row + t) : 0.f;
+        if (FUSE && live)
+#pragma unroll
+            for (int t = 0; t < 3; ++t) pnew[3 * row + t] = xi[t];
         float acc[3] = {0.f, 0.f, 0.f}, dg[3] = {0.f, 0.f, 0.f};
         for (int k = 0; k < w; k += CH) {
             const int *cs;
@@ -1223,7 +1236,7 @@ __global__ void __launch_bounds__(kThreads)
                 if (j < nsl) {
                     c[j] = cs[j * 32 + lane];
 #pragma unroll
-                    for (int t = 0; t < 3; ++t) xj[j][t] = __ldg(p + 3 * (int64_t)c[j] + t);
+                    for (int t = 0; t < 3; ++t) xj[j][t] = pval(3 * (int64_t)c[j] + t);
                 }
 #pragma unroll
             for (int j = 0; j < CH; ++j)
@@ -1279,7 +1292,8 @@ __global__ void __launch_bounds__(kThreads)
 
 constexpr int kSymbSlots = 2, kSymbStages = 4;
 using SymbLayout = SymBulk<kSymbSlots, kSymbStages>;
-#define k_cg_spmv_sym k_cg_spmv_symb<kSymbSlots, kSymbStages, true>
+#define k_cg_spmv_sym k_cg_spmv_symb<kSymbSlots, kSymbStages, true, false>
+#define k_cg_spmv_sym_fused k_cg_spmv_symb<kSymbSlots, kSymbStages, true, true>
 
 // Grid of a bulk-staged kernel: its resident CTAs with `smem` bytes of
 // dynamic shared memory each, capped by the slices.  The first call per
@@ -1306,11 +1320,16 @@ static int staged_grid(K kern, int smem, int64_t ns)
     return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)std::max(per_sm, 1) * sm_count()));
 }
 
-static void launch_cg_spmv_sym(const SellView<float> &U, const float *p, float *q4, KState *S, double *pd,
-                               float *pf, unsigned *tk, cudaStream_t st)
+// fuse: z, pA, pB as k_cg_spmv_symb's FUSE form; else p = pA
+static void launch_cg_spmv_sym(bool fuse, const SellView<float> &U, const float *z, const float *pA, float *pB,
+                               float *q4, KState *S, double *pd, float *pf, unsigned *tk, cudaStream_t st)
 {
-    k_cg_spmv_sym<<<staged_grid(k_cg_spmv_sym, SymbLayout::kSmem, U.ns), kThreads, SymbLayout::kSmem, st>>>(
-        U, p, q4, S, pd, pf, tk);
+    if (fuse)
+        k_cg_spmv_sym_fused<<<staged_grid(k_cg_spmv_sym_fused, SymbLayout::kSmem, U.ns), kThreads, SymbLayout::kSmem,
+                              st>>>(U, z, pA, pB, q4, S, pd, pf, tk);
+    else
+        k_cg_spmv_sym<<<staged_grid(k_cg_spmv_sym, SymbLayout::kSmem, U.ns), kThreads, SymbLayout::kSmem, st>>>(
+            U, nullptr, pA, nullptr, q4, S, pd, pf, tk);
 }
 
 // Reproducible form of the symmetric product (the BiCGSTAB inner iterations,
@@ -1903,21 +1922,27 @@ static int bicg_chunk_ilu(const SellView<double> &A, const Ilu0 &ilu, int chunk,
 
 // One chunk of FP32 CG iterations with the symmetric (upper-half) matrix:
 // dir, product into q4 with <p, Ap> and alpha, update (reads and clears q4).
-static int cg_chunk_sym(const SellView<float> &U, int chunk, int64_t nb, float *x, float *r, float *z, float *p,
-                        float *q4, const float *dinv, int pc, KState *S, double *pd, float *pf, unsigned *tk,
-                        double tol, double delta, int itrmax, cudaStream_t st)
+static int cg_chunk_sym(const SellView<float> &U, bool fuse, int chunk, int64_t nb, float *x, float *r, float *z,
+                        float *pA, float *pB, float *q4, const float *dinv, int pc, KState *S, double *pd, float *pf,
+                        unsigned *tk, double tol, double delta, int itrmax, cudaStream_t st)
 {
     const int64_t n = nb * 3;
     const int gd = resident_grid(k_cg_dir<float>, (n + 31) / 32);
     const int gu = resident_grid(k_cg_update<3, float, 4>, (nb + 31) / 32);
     for (int it = 0; it < chunk; ++it) {
-        k_cg_dir<float><<<gd, kThreads, 0, st>>>(n, z, p, S);
-        launch_cg_spmv_sym(U, p, q4, S, pd, pf, tk, st);
-        k_cg_update<3, float, 4><<<gu, kThreads, 0, st>>>(nb, x, r, z, p, p, q4, dinv, pc, S, pd, pf, tk, tol,
-                                                          delta, itrmax);
+        if (fuse) {  // direction update inside the product (ping-pong pA / pB)
+            launch_cg_spmv_sym(true, U, z, pA, pB, q4, S, pd, pf, tk, st);
+            k_cg_update<3, float, 4><<<gu, kThreads, 0, st>>>(nb, x, r, z, pA, pB, q4, dinv, pc, S, pd, pf, tk, tol,
+                                                              delta, itrmax);
+        } else {
+            k_cg_dir<float><<<gd, kThreads, 0, st>>>(n, z, pA, S);
+            launch_cg_spmv_sym(false, U, nullptr, pA, nullptr, q4, S, pd, pf, tk, st);
+            k_cg_update<3, float, 4><<<gu, kThreads, 0, st>>>(nb, x, r, z, pA, pA, q4, dinv, pc, S, pd, pf, tk, tol,
+                                                              delta, itrmax);
+        }
     }
     PFG_CUDA(cudaGetLastError());
-    return 3 * chunk;
+    return (fuse ? 2 : 3) * chunk;
 }
 
 // One chunk of FP32 BiCGSTAB iterations with the symmetric matrix (the
@@ -1968,7 +1993,9 @@ SolveResult Krylov::solve(DevMatrix &A, const double *b, double *x, const KConfi
     if (cfg.reliable_delta <= 0.0 || cfg.reliable_delta >= 1.0) cfg.reliable_delta = 0.1;
     // update_mode 0 (auto): separate streaming passes.  Measured on GB300 at
     // 3.09M DOF: FP64 CG 894 ms separate vs 1165 ms fused (the fused gather
-    // doubles the work of the FP64-pipe-bound SpMV), FP32 CG 430 vs 448 ms.
+    // doubles the work of the FP64-pipe-bound SpMV), FP32 CG 430 vs 448 ms;
+    // mixed CG from the symmetric copy 257.6-259.1 vs 255.3-257.0 ms (the
+    // gathers of z and p_old cost about what the direction pass saves).
     // Preconditioned BiCGSTAB exists only in the separate form.
     if (cfg.fuse != 0 && cfg.fuse != 1) cfg.fuse = 0;
     if (cfg.algorithm == PFG_ALG_BICGSTAB && cfg.precond != PFG_PC_NONE) cfg.fuse = 0;
@@ -2209,8 +2236,11 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
             PFG_CUDA(cudaMemsetAsync(fx_.p, 0, (size_t)A.nb * 3 * sizeof(unsigned long long), st));
         }
     }
-    if (sym)  // (the first call per kernel sets a kernel attribute: outside capture)
-        cg ? staged_grid(k_cg_spmv_sym, SymbLayout::kSmem, A.ns_u) : staged_grid(k_spmv_symfx, SymbLayout::kSmem, A.ns_u);
+    if (sym) {  // (the first call per kernel sets a kernel attribute: outside capture)
+        staged_grid(k_cg_spmv_sym, SymbLayout::kSmem, A.ns_u);
+        staged_grid(k_cg_spmv_sym_fused, SymbLayout::kSmem, A.ns_u);
+        staged_grid(k_spmv_symfx, SymbLayout::kSmem, A.ns_u);
+    }
     const uint64_t key = graph_key(cg ? 3 : 4, A, x, cfg);
     if (!graph_ || graph_key_ != key) {
         if (graph_) cudaGraphExecDestroy(graph_);
@@ -2220,7 +2250,8 @@ SolveResult Krylov::run_mixed(DevMatrix &A, const double *b, double *x, const KC
             const bool fz = cfg.fuse != 0;
             const int ch = cfg.graph_chunk;
             if (sym && cg)
-                nk = cg_chunk_sym(sell_upper(A), ch, A.nb, x32_.p, r32_.p, z32_.p, pA32_.p, y4_.p, dinv32_.p,
+                nk = cg_chunk_sym(sell_upper(A), fz, ch, A.nb, x32_.p, r32_.p, z32_.p, pA32_.p, pB32_.p, y4_.p,
+                                  dinv32_.p,
                                   cfg.precond, state_.p, partials_.p, partials32_.p, ticket_.p, cfg.relative_er,
                                   cfg.reliable_delta, cfg.itrmax, st);
             else if (sym)
@@ -2532,7 +2563,8 @@ void Krylov::profile(DevMatrix &A, int kernel, int reps, cudaStream_t st, double
                                                                               nullptr);
             break;
         case 8:
-            launch_cg_spmv_sym(sell_upper(A), x32.p, y4_.p, state_.p, partials_.p, partials32_.p, ticket_.p, st);
+            launch_cg_spmv_sym(false, sell_upper(A), nullptr, x32.p, nullptr, y4_.p, state_.p, partials_.p,
+                               partials32_.p, ticket_.p, st);
             break;
         case 11:
             k_cg_spmv_sym_t<2, 4><<<resident_grid(k_cg_spmv_sym_t<2, 4>, A.ns_u), kThreads, 0, st>>>(

@@ -63,6 +63,19 @@ def test_symmetric_storage_matches_oracle(cuda, algorithm, pc):
     assert _rel(x, xf) <= 1e-9
 
 
+@pytest.mark.parametrize("pc", ["BlockJacobi", None])
+def test_symmetric_cg_fused_direction_matches_oracle(cuda, pc):
+    """update_mode "fused": the direction update p = z + beta p rides in the
+    symmetric product (ping-pong p buffers); same bar as the separate form."""
+    p, xo = _system(12, seed=9)
+    s = _solver(p)
+    s.relative_er = 1e-12
+    x = s.solve(algorithm="CG", preconditioning=pc, precision="mixed", stop_rule="true_relative",
+                storage="symmetric", update_mode="fused")
+    assert s.last_info["status"] == 0 and s.last_info["fallback"] == 0, s.last_info
+    assert _rel(x, xo) <= 1e-8, _rel(x, xo)
+
+
 def test_symmetric_storage_larger_mesh_twice(cuda):
     """30^3: two symmetric-storage mixed CG solves in a row reach 1e-10 and
     agree with the FP64 GPU solve to 1e-8 (the second reuses the upper copy)."""
