@@ -123,6 +123,192 @@ static void sym_eig(int n, std::vector<double> &A, std::vector<double> &w)
     }
 }
 
+// The lowest k eigenpairs of a symmetric A (n x n, column-major; destroyed):
+// Householder reduction to tridiagonal T = Q^T A Q without accumulating Q,
+// T's eigenvalues by the implicit QL iteration without vectors (tql1), the k
+// wanted eigenvectors of T by inverse iteration (Peters & Wilkinson, "The
+// calculation of specified eigenvectors by inverse iteration", Handbook for
+// Automatic Computation II (1971); the scheme of LAPACK's dstein: tridiagonal
+// LU with partial pivoting, tiny pivots replaced by eps ||T||, shifts of
+// coincident eigenvalues spread by 10 eps ||T||, modified Gram-Schmidt against
+// the earlier vectors of a cluster, i.e. of eigenvalues within 1e-3 ||T||),
+// and the back transformation Q y by the stored reflectors.  About a third of
+// the work of sym_eig at n = 72, k = 24 (no n x n accumulation of Q).
+// w: all n eigenvalues ascending; Y: n x k, column j the eigenvector of w[j].
+static void sym_eig_lowest(int n, std::vector<double> &A, int k, std::vector<double> &w, std::vector<double> &Y)
+{
+    auto a = [&](int i, int j) -> double & { return A[(size_t)j * n + i]; };
+    std::vector<double> d(n), e(n, 0.0), V((size_t)n * n, 0.0), beta(n, 0.0), v(n), p(n), q(n);
+    for (int j = 0; j + 2 < n; ++j) {
+        double alpha = 0.0;
+        for (int i = j + 1; i < n; ++i) alpha += a(i, j) * a(i, j);
+        alpha = std::sqrt(alpha);
+        if (alpha == 0.0) continue;
+        if (a(j + 1, j) > 0) alpha = -alpha;
+        for (int i = 0; i < n; ++i) v[i] = 0.0;
+        for (int i = j + 1; i < n; ++i) v[i] = a(i, j);
+        v[j + 1] -= alpha;
+        double vv = 0.0;
+        for (int i = j + 1; i < n; ++i) vv += v[i] * v[i];
+        if (vv == 0.0) continue;
+        const double bt = 2.0 / vv;
+        // p = beta A v as a sum of columns (contiguous, vectorisable loops)
+        for (int i = j; i < n; ++i) p[i] = 0.0;
+        for (int l = j + 1; l < n; ++l) {
+            const double vl = bt * v[l];
+            const double *al = &A[(size_t)l * n];
+            for (int i = j; i < n; ++i) p[i] += al[i] * vl;
+        }
+        double K = 0.0;
+        for (int i = j + 1; i < n; ++i) K += v[i] * p[i];
+        K *= 0.5 * bt;
+        for (int i = j; i < n; ++i) q[i] = p[i] - K * v[i];
+        for (int c = j; c < n; ++c)
+            for (int r = j; r < n; ++r) a(r, c) -= v[r] * q[c] + q[r] * v[c];
+        for (int i = j + 1; i < n; ++i) V[(size_t)j * n + i] = v[i];
+        beta[j] = bt;
+    }
+    double tnorm = 0.0;
+    for (int i = 0; i < n; ++i) {
+        d[i] = a(i, i);
+        if (i + 1 < n) e[i] = a(i + 1, i);
+    }
+    for (int i = 0; i < n; ++i)
+        tnorm = std::max(tnorm, std::fabs(d[i]) + (i > 0 ? std::fabs(e[i - 1]) : 0.0) + std::fabs(e[i]));
+    // eigenvalues: implicit QL on copies of (d, e), no vectors
+    const double eps = 2.220446049250313e-16;
+    {
+        std::vector<double> dd = d, ee = e;
+        ee[n - 1] = 0.0;
+        for (int l = 0; l < n; ++l) {
+            for (int iter = 0; iter < 200; ++iter) {
+                int m = l;
+                for (; m < n - 1; ++m) {
+                    const double s = std::fabs(dd[m]) + std::fabs(dd[m + 1]);
+                    if (std::fabs(ee[m]) <= eps * s) break;
+                }
+                if (m == l) break;
+                double g = (dd[l + 1] - dd[l]) / (2.0 * ee[l]);
+                double r = std::sqrt(g * g + 1.0);
+                g = dd[m] - dd[l] + ee[l] / (g + (g >= 0 ? r : -r));
+                double s = 1.0, c = 1.0, pp = 0.0;
+                bool underflow = false;
+                for (int i = m - 1; i >= l; --i) {
+                    const double f = s * ee[i], b = c * ee[i];
+                    r = std::sqrt(f * f + g * g);
+                    ee[i + 1] = r;
+                    if (r == 0.0) {
+                        dd[i + 1] -= pp;
+                        ee[m] = 0.0;
+                        underflow = true;
+                        break;
+                    }
+                    s = f / r;
+                    c = g / r;
+                    g = dd[i + 1] - pp;
+                    r = (dd[i] - g) * s + 2.0 * c * b;
+                    pp = s * r;
+                    dd[i + 1] = g + pp;
+                    g = c * r - b;
+                }
+                if (underflow) continue;
+                dd[l] -= pp;
+                ee[l] = g;
+                ee[m] = 0.0;
+            }
+        }
+        std::sort(dd.begin(), dd.end());
+        w = dd;
+    }
+    // inverse iteration for the k lowest
+    const int kk = std::min(k, n);
+    Y.assign((size_t)n * kk, 0.0);
+    const double tiny = eps * std::max(tnorm, 1e-300);
+    const double ortol = 1e-3 * tnorm, pertol = 10.0 * eps * tnorm;
+    std::vector<double> dl(n), dg(n), du(n), du2(n), x(n), Yt((size_t)n * kk);  // Yt: T's eigenvectors
+    std::vector<char> piv(n);
+    int cluster0 = 0;
+    double prev = 0.0;
+    for (int j = 0; j < kk; ++j) {
+        double lam = w[j];
+        if (j > 0) {
+            if (w[j] - w[j - 1] > ortol) cluster0 = j;
+            if (lam <= prev + pertol) lam = prev + pertol;  // distinct shifts inside a cluster
+        }
+        prev = lam;
+        // LU of T - lam I with partial pivoting (U: diagonal dg, superdiagonals du, du2)
+        for (int i = 0; i < n; ++i) {
+            dg[i] = d[i] - lam;
+            dl[i] = du[i] = (i + 1 < n) ? e[i] : 0.0;
+            du2[i] = 0.0;
+        }
+        for (int i = 0; i + 1 < n; ++i) {
+            if (std::fabs(dg[i]) >= std::fabs(dl[i])) {
+                piv[i] = 0;
+                if (std::fabs(dg[i]) < tiny) dg[i] = dg[i] < 0 ? -tiny : tiny;
+                const double f = dl[i] / dg[i];
+                dl[i] = f;
+                dg[i + 1] -= f * du[i];
+            } else {
+                piv[i] = 1;
+                const double f = dg[i] / dl[i];
+                dg[i] = dl[i];
+                dl[i] = f;
+                const double t = du[i];
+                du[i] = dg[i + 1];
+                dg[i + 1] = t - f * dg[i + 1];
+                if (i + 2 < n) {
+                    du2[i] = du[i + 1];
+                    du[i + 1] = -f * du[i + 1];
+                }
+            }
+        }
+        if (std::fabs(dg[n - 1]) < tiny) dg[n - 1] = dg[n - 1] < 0 ? -tiny : tiny;
+        // start: a fixed pseudo-random vector (different per j)
+        for (int i = 0; i < n; ++i) {
+            uint64_t h = (uint64_t)(j + 1) * 0x9e3779b97f4a7c15ull ^ ((uint64_t)i * 0xbf58476d1ce4e5b9ull);
+            h ^= h >> 31;
+            h *= 0x94d049bb133111ebull;
+            h ^= h >> 29;
+            x[i] = (double)(h >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+        }
+        for (int it = 0; it < 3; ++it) {
+            for (int i = 0; i + 1 < n; ++i) {  // L^-1 (with the row interchanges)
+                if (piv[i]) std::swap(x[i], x[i + 1]);
+                x[i + 1] -= dl[i] * x[i];
+            }
+            for (int i = n - 1; i >= 0; --i) {  // U^-1
+                double t = x[i];
+                if (i + 1 < n) t -= du[i] * x[i + 1];
+                if (i + 2 < n) t -= du2[i] * x[i + 2];
+                x[i] = t / dg[i];
+            }
+            for (int c = cluster0; c < j; ++c) {  // orthogonal to the cluster's earlier vectors
+                const double *yc = &Yt[(size_t)c * n];
+                double s = 0.0;
+                for (int i = 0; i < n; ++i) s += yc[i] * x[i];
+                for (int i = 0; i < n; ++i) x[i] -= s * yc[i];
+            }
+            double nrm = 0.0;
+            for (int i = 0; i < n; ++i) nrm += x[i] * x[i];
+            nrm = std::sqrt(nrm);
+            if (!(nrm > 0.0) || !std::isfinite(nrm)) nrm = 1.0;
+            for (int i = 0; i < n; ++i) x[i] /= nrm;
+        }
+        std::copy(x.begin(), x.end(), Yt.begin() + (size_t)j * n);
+        // back transformation: y <- H_0 (H_1 (... (H_{n-3} y)))
+        for (int jj = n - 3; jj >= 0; --jj) {
+            if (beta[jj] == 0.0) continue;
+            const double *vj = &V[(size_t)jj * n];
+            double s = 0.0;
+            for (int i = jj + 1; i < n; ++i) s += vj[i] * x[i];
+            s *= beta[jj];
+            for (int i = jj + 1; i < n; ++i) x[i] -= s * vj[i];
+        }
+        std::copy(x.begin(), x.end(), Y.begin() + (size_t)j * n);
+    }
+}
+
 // B = L L^T (lower L, column-major, in place of B's lower triangle) when every
 // pivot exceeds rank_tol times the largest diagonal entry; false otherwise.
 static bool cholesky_well_posed(int m, std::vector<double> &B, double rank_tol)
@@ -130,16 +316,20 @@ static bool cholesky_well_posed(int m, std::vector<double> &B, double rank_tol)
     double dmax = 0.0;
     for (int i = 0; i < m; ++i) dmax = std::max(dmax, B[(size_t)i * m + i]);
     if (!(dmax > 0.0)) return false;
+    // right-looking: scale column j, then update the trailing columns (each
+    // update a contiguous column axpy)
     for (int j = 0; j < m; ++j) {
-        double d = B[(size_t)j * m + j];
-        for (int l = 0; l < j; ++l) d -= B[(size_t)l * m + j] * B[(size_t)l * m + j];
+        double *bj = &B[(size_t)j * m];
+        const double d = bj[j];
         if (!(d > rank_tol * dmax)) return false;
         const double ljj = std::sqrt(d);
-        B[(size_t)j * m + j] = ljj;
-        for (int i = j + 1; i < m; ++i) {
-            double v = B[(size_t)j * m + i];
-            for (int l = 0; l < j; ++l) v -= B[(size_t)l * m + i] * B[(size_t)l * m + j];
-            B[(size_t)j * m + i] = v / ljj;
+        bj[j] = ljj;
+        const double inv = 1.0 / ljj;
+        for (int i = j + 1; i < m; ++i) bj[i] *= inv;
+        for (int c = j + 1; c < m; ++c) {
+            double *bc = &B[(size_t)c * m];
+            const double f = bj[c];
+            for (int i = c; i < m; ++i) bc[i] -= bj[i] * f;
         }
     }
     return true;
@@ -164,39 +354,51 @@ int small_generalized_eig(int m, const double *Ain, const double *Bin, int k, do
         // Otherwise B's eigendecomposition below drops its null directions.
         std::vector<double> L = B;
         if (cholesky_well_posed(m, L, rank_tol)) {
-            auto l = [&](int i, int j) { return L[(size_t)j * m + i]; };
-            // W = L^-1 (S A S): forward substitution on each column
-            std::vector<double> W((size_t)m * m);
-            for (int c = 0; c < m; ++c)
-                for (int i = 0; i < m; ++i) {
-                    double v = 0.5 * (Ain[(size_t)c * m + i] + Ain[(size_t)i * m + c]) * s[i] * s[c];
-                    for (int q = 0; q < i; ++q) v -= l(i, q) * W[(size_t)c * m + q];
-                    W[(size_t)c * m + i] = v / l(i, i);
+            // column-oriented forward substitution: x <- L^-1 x (each step a
+            // contiguous axpy down column q of L)
+            auto lsolve = [&](double *x) {
+                for (int q = 0; q < m; ++q) {
+                    const double *lq = &L[(size_t)q * m];
+                    const double xq = x[q] / lq[q];
+                    x[q] = xq;
+                    for (int i = q + 1; i < m; ++i) x[i] -= lq[i] * xq;
                 }
-            // A' = W L^-T = (L^-1 W^T)^T: forward substitution on W's rows
-            std::vector<double> Ap((size_t)m * m);
-            for (int r = 0; r < m; ++r)
-                for (int i = 0; i < m; ++i) {
-                    double v = W[(size_t)i * m + r];
-                    for (int q = 0; q < i; ++q) v -= l(i, q) * Ap[(size_t)q * m + r];
-                    Ap[(size_t)i * m + r] = v / l(i, i);
-                }
-            for (int c = 0; c < m; ++c)
+            };
+            // W = L^-1 (S A S), column by column
+            std::vector<double> W((size_t)m * m), Ap((size_t)m * m);
+            for (int c = 0; c < m; ++c) {
+                double *wc = &W[(size_t)c * m];
+                for (int i = 0; i < m; ++i) wc[i] = 0.5 * (Ain[(size_t)c * m + i] + Ain[(size_t)i * m + c]) * s[i] * s[c];
+                lsolve(wc);
+            }
+            // A' = W L^-T = (L^-1 W^T)^T: the columns of W^T, solved, are A''s rows
+            for (int r = 0; r < m; ++r) {
+                double *ar = &Ap[(size_t)r * m];
+                for (int i = 0; i < m; ++i) ar[i] = W[(size_t)i * m + r];
+                lsolve(ar);
+            }
+            for (int c = 0; c < m; ++c)  // (Ap holds A'^T; symmetrise)
                 for (int i = 0; i < c; ++i) {
                     const double v = 0.5 * (Ap[(size_t)c * m + i] + Ap[(size_t)i * m + c]);
                     Ap[(size_t)c * m + i] = Ap[(size_t)i * m + c] = v;
                 }
-            std::vector<double> mu;
-            sym_eig(m, Ap, mu);
+            std::vector<double> LT((size_t)m * m);  // L^T, for column-oriented back substitution
+            for (int c = 0; c < m; ++c)
+                for (int i = 0; i < m; ++i) LT[(size_t)i * m + c] = L[(size_t)c * m + i];
+            std::vector<double> mu, Y;
             const int kk = std::min(k, m);
+            sym_eig_lowest(m, Ap, kk, mu, Y);
             for (int j = 0; j < kk; ++j) {
                 lam[j] = mu[j];
-                // y = column j of the eigenvectors; C_j = S L^-T y (back substitution)
+                // y = column j of the eigenvectors; C_j = S L^-T y (back
+                // substitution on L^T, column-oriented)
                 double *cj = C + (size_t)j * m;
+                for (int i = 0; i < m; ++i) cj[i] = Y[(size_t)j * m + i];
                 for (int i = m - 1; i >= 0; --i) {
-                    double v = Ap[(size_t)j * m + i];
-                    for (int q = i + 1; q < m; ++q) v -= l(q, i) * cj[q];
-                    cj[i] = v / l(i, i);
+                    const double *lti = &LT[(size_t)i * m];
+                    const double ci = cj[i] / lti[i];
+                    cj[i] = ci;
+                    for (int q = 0; q < i; ++q) cj[q] -= lti[q] * ci;
                 }
                 for (int i = 0; i < m; ++i) cj[i] *= s[i];
             }
@@ -302,6 +504,12 @@ __device__ __forceinline__ void st_row(double *p, const double (&v)[PW])
 #pragma unroll
     for (int u = 0; u < 4; ++u) reinterpret_cast<double2 *>(p)[u] = make_double2(v[2 * u], v[2 * u + 1]);
 }
+__device__ __forceinline__ void st_row(float2 *p, const float2 (&v)[PW])
+{
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+        reinterpret_cast<float4 *>(p)[u] = make_float4(v[2 * u].x, v[2 * u].y, v[2 * u + 1].x, v[2 * u + 1].y);
+}
 // The same from shared memory (plain loads: __ldg is for global memory).
 __device__ __forceinline__ void lds_row(const float *p, float (&v)[PW])
 {
@@ -360,12 +568,34 @@ struct DFAcc {
         lo = __fadd_rn(lo, __fadd_rn(err, e));
     }
     __device__ double get() const { return (double)hi + (double)lo; }
+    // the sum as a normalised (hi, lo) pair: TwoSum of the two parts (FP32 only)
+    __device__ float2 get2() const
+    {
+        const float s = __fadd_rn(hi, lo);
+        const float z = __fsub_rn(s, hi);
+        return make_float2(s, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, z)), __fsub_rn(lo, z)));
+    }
 };
 
 __device__ __forceinline__ float2 df_split(double x)
 {
     const float h = __double2float_rn(x);
     return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+__device__ __forceinline__ double df_value(float2 v) { return (double)v.x + (double)v.y; }
+
+// a + b of two double-float numbers (TwoSum of the heads, the tails added,
+// renormalised by a second TwoSum)
+__device__ __forceinline__ float2 df_add(float2 a, float2 b)
+{
+    const float s = __fadd_rn(a.x, b.x);
+    const float z = __fsub_rn(s, a.x);
+    float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, z)), __fsub_rn(b.x, z));
+    e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+    const float t = __fadd_rn(s, e);
+    const float z2 = __fsub_rn(t, s);
+    return make_float2(t, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z2)), __fsub_rn(e, z2)));
 }
 
 // Y = A X for every panel (one warp per (slice, panel), one lane per block
@@ -420,21 +650,24 @@ __global__ void __launch_bounds__(kT) k_spmm(SellView<T> A, int np, const T *__r
 }
 
 // ---- double-float forms of the SpMM and the linear combinations (mixed
-// second phase).  Their operands are converted to (hi, lo) float pairs in one
-// pass each (k_to_df: one FP64 subtraction per value), so the inner loops are
-// FP32 arithmetic only; splitting each operand where it is used put a
-// conversion per use on the FP64 pipe and was slower than FP64 itself.
+// second phase).  That phase keeps its panels and images as (hi, lo) float
+// pairs: the producers (SpMM, linear combinations, preconditioner, residual)
+// write pairs, so the inner loops are FP32 arithmetic only and no conversion
+// pass runs per iteration; only the matrices' FP64 values are split, once
+// (k_to_df).  Splitting FP64 operands where they are used put a conversion
+// per use on the FP64 pipe and was slower than FP64 itself; converting them
+// in a pass before every use cost 16 % of a double-float iteration.
 __global__ void k_to_df(int64_t len, const double *__restrict__ a, float2 *__restrict__ b)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
         b[i] = df_split(a[i]);
 }
 
-// Y = A X with A's sliced values (vdf, A's slot layout) and the panels X in
-// double-float; Y in FP64.  Layout and warp mapping as k_spmm.
+// Y = A X with A's sliced values (vdf, A's slot layout), the panels X and Y in
+// double-float.  Layout and warp mapping as k_spmm.
 template <int BS>
 __global__ void __launch_bounds__(kT) k_spmm_df(SellView<double> A, const float2 *__restrict__ vdf, int np,
-                                                const float2 *__restrict__ X, double *__restrict__ Y,
+                                                const float2 *__restrict__ X, float2 *__restrict__ Y,
                                                 const uint8_t *__restrict__ fixed)
 {
     const int lane = threadIdx.x & 31;
@@ -474,20 +707,20 @@ __global__ void __launch_bounds__(kT) k_spmm_df(SellView<double> A, const float2
             for (int r = 0; r < BS; ++r) {
                 const int64_t i = (int64_t)BS * row + r;
                 const bool f = fixed && fixed[i];
-                double yv[PW];
+                float2 yv[PW];
 #pragma unroll
-                for (int c = 0; c < PW; ++c) yv[c] = f ? 0.0 : acc[r][c].get();
+                for (int c = 0; c < PW; ++c) yv[c] = f ? make_float2(0.f, 0.f) : acc[r][c].get2();
                 st_row(Y + ((int64_t)q * n + i) * PW, yv);
             }
         }
     }
 }
 
-// k_lincomb with the blocks and the coefficients in double-float; outputs FP64.
+// k_lincomb with the blocks, the coefficients and the results in double-float.
 __global__ void __launch_bounds__(kT)
     k_lincomb_df(int64_t n, int k, int nblk, const float2 *__restrict__ X, const float2 *__restrict__ W,
-                 const float2 *__restrict__ P, const double *__restrict__ C, double *__restrict__ Xn,
-                 double *__restrict__ Pn)
+                 const float2 *__restrict__ P, const double *__restrict__ C, float2 *__restrict__ Xn,
+                 float2 *__restrict__ Pn)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     float2 *sC = (float2 *)smraw;
@@ -527,11 +760,11 @@ __global__ void __launch_bounds__(kT)
                     }
                 }
             }
-            double pv[PW], xv[PW];
+            float2 pv[PW], xv[PW];
 #pragma unroll
             for (int o = 0; o < PW; ++o) {
-                pv[o] = ap[o].get();
-                xv[o] = ax[o].get() + pv[o];
+                pv[o] = ap[o].get2();
+                xv[o] = df_add(ax[o].get2(), pv[o]);
             }
             st_row(Pn + ((int64_t)qo * n + row) * PW, pv);
             st_row(Xn + ((int64_t)qo * n + row) * PW, xv);
@@ -557,7 +790,8 @@ struct GramAcc<float> {
 };
 
 // Staged operand type and accumulator of the Gram kernel per storage type:
-// FP32 panels with compensated FP32 sums, FP64 panels in double-float.
+// FP32 panels (plain or compensated FP32 sums), FP64 panels (FP64), double-
+// float panels (double-float sums).
 template <typename T, bool DF>
 struct GramArith;
 // FP32 panels (the mixed first phase, which stops at a 1e-4 residual): plain
@@ -584,10 +818,10 @@ struct GramArith<double, false> {
     __device__ static double none() { return 0.0; }
 };
 template <>
-struct GramArith<double, true> {
+struct GramArith<float2, true> {  // panels already in double-float (mixed second phase)
     using Stage = float2;
     using Acc = DFAcc;
-    __device__ static float2 stage(double x) { return df_split(x); }
+    __device__ static float2 stage(float2 x) { return x; }
     __device__ static float2 none() { return make_float2(0.f, 0.f); }
 };
 
@@ -614,11 +848,9 @@ __device__ __forceinline__ void gram_stage16(const double *src, double *dst)
 {
     *reinterpret_cast<double2 *>(dst) = __ldg(reinterpret_cast<const double2 *>(src));
 }
-__device__ __forceinline__ void gram_stage16(const double *src, float2 *dst)  // split into double-float
+__device__ __forceinline__ void gram_stage16(const float2 *src, float2 *dst)
 {
-    const double2 w = __ldg(reinterpret_cast<const double2 *>(src));
-    const float2 a = df_split(w.x), b = df_split(w.y);
-    *reinterpret_cast<float4 *>(dst) = make_float4(a.x, a.y, b.x, b.y);
+    *reinterpret_cast<float4 *>(dst) = __ldg(reinterpret_cast<const float4 *>(src));
 }
 // four consecutive staged values (16- or 32-byte aligned)
 __device__ __forceinline__ void gram_lds4(const float *p, float (&v)[kGramSub])
@@ -661,8 +893,8 @@ __device__ __forceinline__ void gram_lds4(const float2 *p, float2 (&v)[kGramSub]
 // loads.  Per staged row a thread reads its 4 values of S and 4 of each image
 // with 16-byte shared loads and does 32 multiply-adds: FP32 for FP32 panels
 // (per CTA row range; the ranges are summed in FP64), FP64 for FP64 panels,
-// or double-float (DF, the mixed mode's second phase) on the FP32 pipe, the
-// operands split once when staged.  Padding columns are staged as they are
+// or double-float (DF: double-float panels of the mixed mode's second phase)
+// on the FP32 pipe.  Padding columns are staged as they are
 // stored and their sums are not written; the sub-tile below the diagonal of
 // a diagonal tile is computed and not written.
 template <typename T, bool DF>
@@ -878,6 +1110,101 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
+// k_residual for double-float panels: R = KX - MX diag(lam) formed in FP64
+// from the (hi, lo) pairs and stored split again; sums as k_residual.
+__global__ void __launch_bounds__(kT)
+    k_residual_df(int64_t n, int k, const float2 *__restrict__ KX, const float2 *__restrict__ MX,
+                  const double *__restrict__ lam, float2 *__restrict__ R, double *part)
+{
+    __shared__ double sred[3 * PW][kT / 32];
+    const int q = blockIdx.y;
+    double rr[PW], mm[PW], mx[PW], lq[PW];
+#pragma unroll
+    for (int c = 0; c < PW; ++c) {
+        rr[c] = mm[c] = mx[c] = 0.0;
+        lq[c] = q * PW + c < k ? lam[q * PW + c] : 0.0;
+    }
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t off = ((int64_t)q * n + row) * PW;
+        float2 kv[PW], mv[PW];
+        ld_row(KX + off, kv);
+        ld_row(MX + off, mv);
+#pragma unroll
+        for (int c = 0; c < PW; ++c) {
+            if (q * PW + c >= k) {
+                kv[c] = make_float2(0.f, 0.f);
+                continue;
+            }
+            const double m = df_value(mv[c]);
+            const double r = df_value(kv[c]) - m * lq[c];
+            kv[c] = df_split(r);
+            rr[c] += r * r;
+            mm[c] += m * m;
+            mx[c] = fmax(mx[c], fabs(r));
+        }
+        st_row(R + off, kv);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < PW; ++c) {
+        double a = warp_sum(rr[c]), b = warp_sum(mm[c]), m = mx[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) {
+            sred[3 * c][wid] = a;
+            sred[3 * c + 1][wid] = b;
+            sred[3 * c + 2][wid] = m;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 * PW) {
+        const int c = threadIdx.x / 3, t = threadIdx.x % 3;
+        if (q * PW + c < k) {
+            double v = 0.0;
+            for (int w = 0; w < (int)(blockDim.x / 32); ++w) v = t == 2 ? fmax(v, sred[3 * c + t][w]) : v + sred[3 * c + t][w];
+            part[(int64_t)blockIdx.x * 3 * k + 3 * (q * PW + c) + t] = v;
+        }
+    }
+}
+
+// k_eig_precond for double-float panels, in double-float arithmetic (the
+// block inverse split once per node).
+template <int BS>
+__global__ void __launch_bounds__(kT)
+    k_eig_precond_df(int64_t nb, int k, const double *__restrict__ dinv, int pc, const float2 *__restrict__ R,
+                     float2 *__restrict__ W, const uint8_t *__restrict__ fixed)
+{
+    const int np = (k + PW - 1) / PW;
+    const int64_t n = nb * BS;
+    for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nb;
+         node += (int64_t)gridDim.x * blockDim.x) {
+        float2 D[BS * BS];
+#pragma unroll
+        for (int e = 0; e < BS * BS; ++e)
+            D[e] = pc == PFG_PC_NONE ? make_float2(e % (BS + 1) == 0 ? 1.f : 0.f, 0.f)
+                                     : df_split(dinv[node * BS * BS + e]);
+        for (int q = 0; q < np; ++q) {
+            float2 rv[BS][PW];
+#pragma unroll
+            for (int i = 0; i < BS; ++i) ld_row(panel_row(R, n, q, (int64_t)BS * node + i), rv[i]);
+#pragma unroll
+            for (int i = 0; i < BS; ++i) {
+                const bool f = fixed && fixed[(int64_t)BS * node + i];
+                float2 wv[PW];
+#pragma unroll
+                for (int c = 0; c < PW; ++c) {
+                    DFAcc a;
+                    a.zero();
+#pragma unroll
+                    for (int j = 0; j < BS; ++j) a.add(D[BS * i + j], rv[j][c]);
+                    wv[c] = f ? make_float2(0.f, 0.f) : a.get2();
+                }
+                st_row(W + ((int64_t)q * n + (int64_t)BS * node + i) * PW, wv);
+            }
+        }
+    }
+}
+
 // W = T R: block Jacobi (BS x BS diagonal blocks of K) per node and column;
 // fixed DOFs zeroed.
 template <int BS, typename T>
@@ -939,11 +1266,16 @@ __global__ void k_random(int64_t n, int k, uint64_t seed, T *__restrict__ X, con
     }
 }
 
-template <typename S, typename D>
-__global__ void k_convert(int64_t len, const S *__restrict__ a, D *__restrict__ b)
+__device__ __forceinline__ float2 to_df32(float x) { return make_float2(x, 0.f); }
+__device__ __forceinline__ double to_f64(float x) { return (double)x; }
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float2 x) { return df_value(x); }
+
+// FP32 panels -> double-float panels (the start of the mixed second phase)
+__global__ void k_f32_to_df(int64_t len, const float *__restrict__ a, float2 *__restrict__ b)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x)
-        b[i] = (D)a[i];
+        b[i] = to_df32(a[i]);
 }
 
 // first nev columns of X (panels) -> column-major n x nev (FP64)
@@ -953,7 +1285,7 @@ __global__ void k_unpanel(int64_t n, int nev, const T *__restrict__ X, double *_
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * nev; i += (int64_t)gridDim.x * blockDim.x) {
         const int j = (int)(i / n);
         const int64_t row = i - (int64_t)j * n;
-        out[i] = (double)X[((int64_t)(j / PW) * n + row) * PW + (j % PW)];
+        out[i] = to_f64(X[((int64_t)(j / PW) * n + row) * PW + (j % PW)]);
     }
 }
 
@@ -988,8 +1320,7 @@ struct Ctx {
     int k, kp, np;
     cudaStream_t st;
     const uint8_t *fixed;
-    bool df = false;  // FP64 panels: Gram, SpMM and linear combinations in double-float (mixed second phase)
-    DevBuf<float2> df_a, df_b, df_c, df_K, df_M;  // converted panels (3) and sliced matrix values
+    DevBuf<float2> df_K, df_M;  // the sliced FP64 matrix values as double-float pairs (mixed second phase)
     const DevMatrix *dfK = nullptr, *dfM = nullptr;
     int launches = 0;
     DevBuf<double> part, gram, C, lam_d, dinv;
@@ -1021,8 +1352,8 @@ static void to_df(Ctx &c, const double *a, float2 *b, int64_t len)
     ++c.launches;
 }
 
-// Y = A X for X already in double-float (Xdf).
-static void spmm_df(Ctx &c, const DevMatrix &A, const float2 *Xdf, double *Y)
+// Y = A X, panels in double-float, A's values as double-float pairs.
+static void spmm_df(Ctx &c, const DevMatrix &A, const float2 *X, float2 *Y)
 {
     const SellView<double> v = A.sell<double>();
     int per = 0;
@@ -1033,49 +1364,43 @@ static void spmm_df(Ctx &c, const DevMatrix &A, const float2 *Xdf, double *Y)
     const int64_t warps = A.ns * c.np;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)std::max(per, 1) * sms()));
     if (A.bs == 3)
-        k_spmm_df<3><<<g, kT, 0, c.st>>>(v, df_values(c, A), c.np, Xdf, Y, c.fixed);
+        k_spmm_df<3><<<g, kT, 0, c.st>>>(v, df_values(c, A), c.np, X, Y, c.fixed);
     else
-        k_spmm_df<1><<<g, kT, 0, c.st>>>(v, df_values(c, A), c.np, Xdf, Y, c.fixed);
+        k_spmm_df<1><<<g, kT, 0, c.st>>>(v, df_values(c, A), c.np, X, Y, c.fixed);
     PFG_CUDA(cudaGetLastError());
     ++c.launches;
-}
-
-template <typename T>
-void spmm(Ctx &c, const DevMatrix &A, const T *X, T *Y);
-
-// KX = K X and MX = M X (X converted once in double-float mode).
-template <typename T>
-void spmm_pair(Ctx &c, const DevMatrix &K, const DevMatrix &M, const T *X, T *KX, T *MX)
-{
-    if constexpr (std::is_same<T, double>::value) {
-        if (c.df) {
-            to_df(c, X, c.df_a.p, c.n * c.kp);
-            spmm_df(c, K, c.df_a.p, KX);
-            spmm_df(c, M, c.df_a.p, MX);
-            return;
-        }
-    }
-    spmm<T>(c, K, X, KX);
-    spmm<T>(c, M, X, MX);
 }
 
 template <typename T>
 void spmm(Ctx &c, const DevMatrix &A, const T *X, T *Y)
 {
-    const SellView<T> v = sell_of<T>(A);
-    int per = 0;
-    if (A.bs == 3)
-        PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm<3, T>, kT, 0));
-    else
-        PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm<1, T>, kT, 0));
-    const int64_t warps = A.ns * c.np;
-    const int g = (int)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)std::max(per, 1) * sms()));
-    if (A.bs == 3)
-        k_spmm<3, T><<<g, kT, 0, c.st>>>(v, c.np, X, Y, c.fixed);
-    else
-        k_spmm<1, T><<<g, kT, 0, c.st>>>(v, c.np, X, Y, c.fixed);
-    PFG_CUDA(cudaGetLastError());
-    ++c.launches;
+    if constexpr (std::is_same<T, float2>::value) {
+        spmm_df(c, A, X, Y);
+    } else {
+        const SellView<T> v = sell_of<T>(A);
+        int per = 0;
+        if (A.bs == 3)
+            PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm<3, T>, kT, 0));
+        else
+            PFG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_spmm<1, T>, kT, 0));
+        const int64_t warps = A.ns * c.np;
+        const int g =
+            (int)std::max<int64_t>(1, std::min<int64_t>((warps + 7) / 8, (int64_t)std::max(per, 1) * sms()));
+        if (A.bs == 3)
+            k_spmm<3, T><<<g, kT, 0, c.st>>>(v, c.np, X, Y, c.fixed);
+        else
+            k_spmm<1, T><<<g, kT, 0, c.st>>>(v, c.np, X, Y, c.fixed);
+        PFG_CUDA(cudaGetLastError());
+        ++c.launches;
+    }
+}
+
+// KX = K X and MX = M X
+template <typename T>
+void spmm_pair(Ctx &c, const DevMatrix &K, const DevMatrix &M, const T *X, T *KX, T *MX)
+{
+    spmm<T>(c, K, X, KX);
+    spmm<T>(c, M, X, MX);
 }
 
 template <typename T>
@@ -1091,7 +1416,9 @@ void gram(Ctx &c, int nblk, const Blocks<T> &B, std::vector<double> &GA, std::ve
     const int g = c.ngrid;
     c.part.ensure((size_t)g * 2 * npairs);
     c.gram.ensure((size_t)2 * npairs);
-    auto kern = (std::is_same<T, double>::value && c.df) ? k_gram<T, true> : k_gram<T, false>;
+    // float2: double-float panels (mixed second phase); float: FP32; double: IEEE FP64
+    constexpr bool kDF = std::is_same<T, float2>::value;
+    auto kern = k_gram<T, kDF>;
     PFG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kern<<<g, threads, smem, c.st>>>(c.n, c.k, nblk, B.X.p, B.W.p, B.P.p, B.KX.p, B.KW.p, B.KP.p, B.MX.p, B.MW.p,
                                      B.MP.p, c.part.p);
@@ -1116,22 +1443,13 @@ void lincomb(Ctx &c, int nblk, const T *X, const T *W, const T *P, T *Xn, T *Pn)
 {
     const int m = nblk * c.k;
     const size_t smem = (size_t)m * c.kp * sizeof(T);  // (a double-float coefficient is 8 bytes too)
-    if constexpr (std::is_same<T, double>::value) {
-        if (c.df) {  // float2 coefficients: the same 8 bytes each
-            const int64_t len = c.n * c.kp;
-            to_df(c, X, c.df_a.p, len);
-            to_df(c, W, c.df_b.p, len);
-            if (nblk == 3) to_df(c, P, c.df_c.p, len);
-            PFG_CUDA(cudaFuncSetAttribute(k_lincomb_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k_lincomb_df<<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, c.df_a.p, c.df_b.p,
-                                                                          c.df_c.p, c.C.p, Xn, Pn);
-            PFG_CUDA(cudaGetLastError());
-            ++c.launches;
-            return;
-        }
+    if constexpr (std::is_same<T, float2>::value) {
+        PFG_CUDA(cudaFuncSetAttribute(k_lincomb_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_lincomb_df<<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, X, W, P, c.C.p, Xn, Pn);
+    } else {
+        PFG_CUDA(cudaFuncSetAttribute(k_lincomb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_lincomb<T><<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, X, W, P, c.C.p, Xn, Pn);
     }
-    PFG_CUDA(cudaFuncSetAttribute(k_lincomb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_lincomb<T><<<grid_for(c.n, kT, sms() * 8), kT, smem, c.st>>>(c.n, c.k, nblk, X, W, P, c.C.p, Xn, Pn);
     PFG_CUDA(cudaGetLastError());
     ++c.launches;
 }
@@ -1177,7 +1495,10 @@ ResInfo residuals(Ctx &c, Blocks<T> &B)
 {
     const int g = std::min(c.ngrid, 1024);
     c.part.ensure((size_t)g * 3 * c.k);
-    k_residual<T><<<dim3(g, c.np), kT, 0, c.st>>>(c.n, c.k, B.KX.p, B.MX.p, c.lam_d.p, B.R.p, c.part.p);
+    if constexpr (std::is_same<T, float2>::value)
+        k_residual_df<<<dim3(g, c.np), kT, 0, c.st>>>(c.n, c.k, B.KX.p, B.MX.p, c.lam_d.p, B.R.p, c.part.p);
+    else
+        k_residual<T><<<dim3(g, c.np), kT, 0, c.st>>>(c.n, c.k, B.KX.p, B.MX.p, c.lam_d.p, B.R.p, c.part.p);
     PFG_CUDA(cudaGetLastError());
     ++c.launches;
     std::vector<double> h((size_t)g * 3 * c.k);
@@ -1209,10 +1530,13 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
           int &iters_left, int &iters_done, double &max_rel, double &ref_r1)
 {
     const size_t len = (size_t)c.n * c.kp;
-    if (start == 0) {
-        k_random<T><<<grid_for((int64_t)len, 256, sms() * 8), 256, 0, c.st>>>(c.n, c.k, cfg.seed, B.X.p, c.fixed);
-        PFG_CUDA(cudaGetLastError());
-        ++c.launches;
+    if constexpr (!std::is_same<T, float2>::value) {
+        if (start == 0) {
+            k_random<T><<<grid_for((int64_t)len, 256, sms() * 8), 256, 0, c.st>>>(c.n, c.k, cfg.seed, B.X.p,
+                                                                                 c.fixed);
+            PFG_CUDA(cudaGetLastError());
+            ++c.launches;
+        }
     }
     const double rank_tol = fp32_phase ? 1e-9 : 1e-13;
     spmm<T>(c, K, B.X.p, B.KX.p);
@@ -1264,12 +1588,18 @@ int phase(Ctx &c, DevMatrix &K, DevMatrix &M, Blocks<T> &B, const EigConfig &cfg
         --iters_left;
         ++iters_done;
         // W = T R, its images
-        if (c.bs == 3)
-            k_eig_precond<3, T><<<grid_for(c.nb, kT, sms() * 8), kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond,
-                                                                                B.R.p, B.W.p, c.fixed);
-        else
-            k_eig_precond<1, T><<<grid_for(c.nb, kT, sms() * 8), kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond,
-                                                                                B.R.p, B.W.p, c.fixed);
+        const int gp = grid_for(c.nb, kT, sms() * 8);
+        if constexpr (std::is_same<T, float2>::value) {
+            if (c.bs == 3)
+                k_eig_precond_df<3><<<gp, kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond, B.R.p, B.W.p, c.fixed);
+            else
+                k_eig_precond_df<1><<<gp, kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond, B.R.p, B.W.p, c.fixed);
+        } else {
+            if (c.bs == 3)
+                k_eig_precond<3, T><<<gp, kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond, B.R.p, B.W.p, c.fixed);
+            else
+                k_eig_precond<1, T><<<gp, kT, 0, c.st>>>(c.nb, c.k, c.dinv.p, cfg.precond, B.R.p, B.W.p, c.fixed);
+        }
         PFG_CUDA(cudaGetLastError());
         ++c.launches;
         spmm_pair<T>(c, K, M, B.W.p, B.KW.p, B.MW.p);
@@ -1329,44 +1659,45 @@ EigResult lobpcg_solve(DevMatrix &K, DevMatrix &M, const uint8_t *fixed, const E
     const size_t len = (size_t)c.n * c.kp;
     int iters_left = cfg.max_itr, iters_done = 0, rc = -1;
     double max_rel = 0.0, ref_r1 = -1.0;
-    Blocks<double> B64;
-    B64.alloc(len);
     build_sell(K, true, cfg.precision == PFG_PREC_MIXED, st);
     build_sell(M, true, cfg.precision == PFG_PREC_MIXED, st);
-    int start = 0;
+    Blocks<double> B64;
+    Blocks<float2> Bdf;
     if (cfg.precision == PFG_PREC_MIXED) {
-        Blocks<float> B32;
-        B32.alloc(len);
-        double r1 = -1.0;
-        rc = phase<float>(c, K, M, B32, cfg, true, 0, iters_left, iters_done, max_rel, r1);
-        res.iterations_fp32 = iters_done;
-        k_convert<float, double><<<grid_for((int64_t)len, 256, sms() * 8), 256, 0, st>>>((int64_t)len, B32.X.p, B64.X.p);
-        PFG_CUDA(cudaGetLastError());
-        ++c.launches;
-        start = 1;
-    }
-    // the mixed mode's second phase: FP64 panels, their SpMM, Gram and linear
-    // combinations in double-float on the FP32 pipe; precision FP64: IEEE FP64
-    c.df = cfg.precision == PFG_PREC_MIXED;
-    if (c.df) {
-        const int64_t len = c.n * c.kp;
-        c.df_a.resize((size_t)len);
-        c.df_b.resize((size_t)len);
-        c.df_c.resize((size_t)len);
+        // FP32 phase, then the second phase with the panels, images, SpMM,
+        // Gram and linear combinations in double-float on the FP32 pipe (the
+        // matrices' FP64 values split once here)
+        {
+            Blocks<float> B32;
+            B32.alloc(len);
+            double r1 = -1.0;
+            rc = phase<float>(c, K, M, B32, cfg, true, 0, iters_left, iters_done, max_rel, r1);
+            res.iterations_fp32 = iters_done;
+            Bdf.alloc(len);
+            k_f32_to_df<<<grid_for((int64_t)len, 256, sms() * 8), 256, 0, st>>>((int64_t)len, B32.X.p, Bdf.X.p);
+            PFG_CUDA(cudaGetLastError());
+            ++c.launches;
+        }
         c.dfK = &K;
         c.dfM = &M;
         c.df_K.resize(K.s64.n);
         c.df_M.resize(M.s64.n);
         to_df(c, K.s64.p, c.df_K.p, (int64_t)K.s64.n);
         to_df(c, M.s64.p, c.df_M.p, (int64_t)M.s64.n);
+        rc = phase<float2>(c, K, M, Bdf, cfg, false, 1, iters_left, iters_done, max_rel, ref_r1);
+    } else {
+        B64.alloc(len);
+        rc = phase<double>(c, K, M, B64, cfg, false, 0, iters_left, iters_done, max_rel, ref_r1);
     }
-    rc = phase<double>(c, K, M, B64, cfg, false, start, iters_left, iters_done, max_rel, ref_r1);
     res.iterations = iters_done;
     res.max_rel_residual = max_rel;
     res.status = rc == 1 ? PFG_OK : PFG_W_NOT_CONVERGED;
     for (int j = 0; j < cfg.nev; ++j) lambda[j] = c.hlam[j];
     if (Xout) {
-        k_unpanel<double><<<grid_for(c.n * cfg.nev, 256, sms() * 8), 256, 0, st>>>(c.n, cfg.nev, B64.X.p, Xout);
+        if (cfg.precision == PFG_PREC_MIXED)
+            k_unpanel<float2><<<grid_for(c.n * cfg.nev, 256, sms() * 8), 256, 0, st>>>(c.n, cfg.nev, Bdf.X.p, Xout);
+        else
+            k_unpanel<double><<<grid_for(c.n * cfg.nev, 256, sms() * 8), 256, 0, st>>>(c.n, cfg.nev, B64.X.p, Xout);
         PFG_CUDA(cudaGetLastError());
         ++c.launches;
     }
