@@ -86,6 +86,8 @@ def lib():
                                    C.POINTER(C.c_int)]
     L.orc_num_threads.restype = C.c_int
     L.orc_crs_spmm.argtypes = [C.c_int64, _i64, _i32, _d, C.c_int64, _d, _d]
+    L.orc_gram_schmidt.argtypes = [C.c_int64, C.c_int64, C.c_void_p]
+    L.orc_gram_schmidt_rm.argtypes = [C.c_int64, C.c_int64, C.c_void_p]
     _LIB = L
     return L
 

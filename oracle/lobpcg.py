@@ -16,7 +16,25 @@ import scipy.linalg as sla
 
 def gram_schmidt(V: np.ndarray) -> np.ndarray:
     """GramSchmidt (SparseClass.f90:2243-2275): column-sequential modified GS,
-    zero columns skipped, each column normalised after projection."""
+    zero columns skipped, each column normalised after projection.  Runs the
+    compiled restatement (``orc_gram_schmidt``, OpenMP) when the oracle
+    library is built, else :func:`gram_schmidt_numpy`."""
+    try:
+        from . import lib
+        L = lib()
+    except Exception:  # library not built: the numpy loop
+        return gram_schmidt_numpy(V)
+    if np.asarray(V).flags.f_contiguous and not np.asarray(V).flags.c_contiguous:
+        out = np.array(V, dtype=np.float64, order="F", copy=True)
+        L.orc_gram_schmidt(out.shape[0], out.shape[1], out.ctypes.data)
+    else:  # row-major: transposed inside the library (a numpy transpose copy is slow)
+        out = np.array(V, dtype=np.float64, order="C", copy=True)
+        L.orc_gram_schmidt_rm(out.shape[0], out.shape[1], out.ctypes.data)
+    return out
+
+
+def gram_schmidt_numpy(V: np.ndarray) -> np.ndarray:
+    """The same in numpy, one column operation at a time."""
     out = np.asfortranarray(V, dtype=np.float64).copy(order="F")  # contiguous columns
     m = out.shape[1]
     for i in range(m):
@@ -37,11 +55,12 @@ def lapack_eig(A, B):
 
 
 def lobpcg_crs(A, B, m: int, max_itr: int = 100000, tol: float = 1e-6, X_init=None, seed: int = 0,
-               return_iters: bool = False):
+               return_iters: bool = False, progress=None):
     """LOBPCG_CRS(A, B, lambda, X, m, MAX_ITR, TOL, X_init) with A, B scipy sparse.
 
     Convergence test as the reference: max|R| / max|R at iteration 1| < TOL
-    (SparseClass.f90:2218-2234).  The random start (``random%randn`` is
+    (SparseClass.f90:2218-2234).  ``progress(it, ratio, lam)``, if given, is
+    called after every iteration (for logging long runs).  The random start (``random%randn`` is
     uniform, RandomClass.f90:265-283) uses a seeded numpy generator here.
     """
     n = A.shape[0]
@@ -87,6 +106,8 @@ def lobpcg_crs(A, B, m: int, max_itr: int = 100000, tol: float = 1e-6, X_init=No
         rmax = np.abs(R).max()
         if it == 1:
             initial_R = rmax
+        if progress is not None:
+            progress(it, rmax / initial_R, lam[:m])
         if rmax / initial_R < tol:
             break
     lam = lam[:m].copy()

@@ -764,6 +764,74 @@ void orc_crs_spmm(int64_t n, const int64_t *row_ptr, const int32_t *col_idx, con
     }
 }
 
+/* GramSchmidt (SparseClass.f90:2243-2275): column-sequential modified
+ * Gram-Schmidt of the n x m column-major V in place; a column that is zero on
+ * entry is skipped, each other column is projected off the columns before it
+ * one at a time (nai = v_j . viold, viold = viold - nai v_j) and normalised.
+ * The projection off v_j and the dot with v_{j+1} share one pass over viold;
+ * the dots are OpenMP reductions (summation order differs from a sequential
+ * loop in the last bits only). */
+void orc_gram_schmidt(int64_t n, int64_t m, double *V)
+{
+    double *viold = malloc((size_t)n * sizeof(double));
+    for (int64_t i = 0; i < m; ++i) {
+        double *vi = V + i * n;
+        double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+        for (int64_t k = 0; k < n; ++k) {
+            viold[k] = vi[k];
+            s += vi[k] * vi[k];
+        }
+        if (s == 0.0) continue;
+        double nai = 0.0;
+        if (i > 0) {
+            const double *v0 = V;
+#pragma omp parallel for reduction(+ : nai) schedule(static)
+            for (int64_t k = 0; k < n; ++k) nai += v0[k] * viold[k];
+        }
+        for (int64_t j = 0; j < i; ++j) {
+            const double *vj = V + j * n;
+            const double *vn = j + 1 < i ? V + (j + 1) * n : viold;  /* next dot, or |viold|^2 */
+            const double a = nai;
+            double t = 0.0;
+#pragma omp parallel for reduction(+ : t) schedule(static)
+            for (int64_t k = 0; k < n; ++k) {
+                const double v = viold[k] - a * vj[k];
+                viold[k] = v;
+                t += vn[k] * v;
+            }
+            nai = t;
+        }
+        /* here nai = |viold|^2 (for i > 0: the last pass dotted viold with itself) */
+        const double nrm = i > 0 ? sqrt(nai) : sqrt(s);
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < n; ++k) vi[k] = viold[k] / nrm;
+    }
+    free(viold);
+}
+
+/* The same for a row-major n x m V (numpy's C order): transposed into a
+ * column-major scratch in 64-row tiles (OpenMP), orthogonalised, and
+ * transposed back. */
+void orc_gram_schmidt_rm(int64_t n, int64_t m, double *V)
+{
+    double *T = malloc((size_t)n * (size_t)m * sizeof(double));
+#pragma omp parallel for schedule(static)
+    for (int64_t r0 = 0; r0 < n; r0 += 64) {
+        const int64_t r1 = r0 + 64 < n ? r0 + 64 : n;
+        for (int64_t c = 0; c < m; ++c)
+            for (int64_t r = r0; r < r1; ++r) T[c * n + r] = V[r * m + c];
+    }
+    orc_gram_schmidt(n, m, T);
+#pragma omp parallel for schedule(static)
+    for (int64_t r0 = 0; r0 < n; r0 += 64) {
+        const int64_t r1 = r0 + 64 < n ? r0 + 64 : n;
+        for (int64_t r = r0; r < r1; ++r)
+            for (int64_t c = 0; c < m; ++c) V[r * m + c] = T[c * n + r];
+    }
+    free(T);
+}
+
 int orc_num_threads(void)
 {
 #ifdef _OPENMP

@@ -223,7 +223,11 @@ def stage_cfg3(n=60, nev=20, block=24, tol=1e-8):
     B = O.CrsOperator(rm, cm, vm)
     _log(f"cfg3: reduced pencil of {A.shape[0]} DOF")
     t = time.time()
-    lam, X, it = OL.lobpcg_crs(A, B, block, max_itr=5000, tol=tol, seed=0, return_iters=True)
+    def progress(i, ratio, lam):
+        if i % 25 == 0:
+            _log(f"cfg3: iteration {i}, max|R| / max|R_1| {ratio:.3e}, lambda_1 {lam[0]:.10g}")
+
+    lam, X, it = OL.lobpcg_crs(A, B, block, max_itr=5000, tol=tol, seed=0, return_iters=True, progress=progress)
     _log(f"cfg3: LOBPCG {it} iterations ({time.time() - t:.0f} s)")
     # relative residuals of the wanted pairs, |K x - lambda M x| / |lambda M x|
     AX, BX = A @ X[:, :nev], B @ X[:, :nev]

@@ -130,6 +130,23 @@ def test_lobpcg_sample_kat():
     assert abs(lam[0] - w[0]) < 1e-7
 
 
+def test_gram_schmidt_compiled_equals_numpy_loop():
+    """GramSchmidt (SparseClass.f90:2243-2275): the compiled restatement
+    (orc_gram_schmidt, both memory orders) equals the numpy loop, skips a zero
+    column and returns orthonormal columns."""
+    rng = np.random.default_rng(11)
+    V = rng.random((3000, 20))
+    V[:, 5] = 0.0
+    ref = L.gram_schmidt_numpy(V)
+    for W in (V, np.asfortranarray(V)):
+        got = L.gram_schmidt(W)
+        assert np.abs(got - ref).max() <= 1e-13
+    keep = [j for j in range(20) if j != 5]
+    Q = ref[:, keep]
+    assert np.abs(Q.T @ Q - np.eye(19)).max() <= 1e-12
+    assert np.all(ref[:, 5] == 0.0)
+
+
 def test_poisson_1d_kat():
     """Tutorial/fem/FEMSolver_PoissonMatrix.f90:18-45 through setCRS(CRS)+solve."""
     n = 100
