@@ -87,7 +87,7 @@ def lib():
     L.orc_num_threads.restype = C.c_int
     L.orc_crs_spmm.argtypes = [C.c_int64, _i64, _i32, _d, C.c_int64, _d, _d]
     L.orc_gram_schmidt.argtypes = [C.c_int64, C.c_int64, C.c_void_p]
-    L.orc_gram_schmidt_rm.argtypes = [C.c_int64, C.c_int64, C.c_void_p]
+    L.orc_gram_schmidt_rm.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p]
     _LIB = L
     return L
 
@@ -311,6 +311,12 @@ class CrsOperator:
         if X.ndim == 1:
             return spmm(self.row_ptr, self.col_idx, self.val, X[:, None])[:, 0]
         return spmm(self.row_ptr, self.col_idx, self.val, X)
+
+    def matmul_into(self, X, out):
+        """out = A X for C-contiguous float64 X and out (n x m), no allocation."""
+        assert X.flags.c_contiguous and out.flags.c_contiguous and X.shape == out.shape
+        lib().orc_crs_spmm(self.shape[0], self.row_ptr, self.col_idx, self.val, X.shape[1], X.reshape(-1),
+                           out.reshape(-1))
 
 
 def pcg(row_ptr, col_idx, val, b, tol=1e-12, maxit=200000, x0=None):

@@ -29,8 +29,21 @@ def gram_schmidt(V: np.ndarray) -> np.ndarray:
         L.orc_gram_schmidt(out.shape[0], out.shape[1], out.ctypes.data)
     else:  # row-major: transposed inside the library (a numpy transpose copy is slow)
         out = np.array(V, dtype=np.float64, order="C", copy=True)
-        L.orc_gram_schmidt_rm(out.shape[0], out.shape[1], out.ctypes.data)
+        L.orc_gram_schmidt_rm(out.shape[0], out.shape[1], out.ctypes.data, None)
     return out
+
+
+def _gram_schmidt_inplace(V: np.ndarray, scratch: np.ndarray) -> None:
+    """gram_schmidt on a C-contiguous V in place (compiled, with a reused scratch)."""
+    from . import lib
+    lib().orc_gram_schmidt_rm(V.shape[0], V.shape[1], V.ctypes.data, scratch.ctypes.data)
+
+
+def _mm_into(A, X, out):
+    if hasattr(A, "matmul_into"):
+        A.matmul_into(X, out)
+    else:
+        out[...] = A @ X
 
 
 def gram_schmidt_numpy(V: np.ndarray) -> np.ndarray:
@@ -90,20 +103,41 @@ def lobpcg_crs(A, B, m: int, max_itr: int = 100000, tol: float = 1e-6, X_init=No
     P = OR @ b_small[:, :m]
     initial_R = None
     it = 0
+    # The loop's n x m and n x 3m arrays live in buffers allocated once: the
+    # same arithmetic as allocating them per iteration, without faulting in
+    # fresh pages of hundreds of MB every iteration at large n.
+    compiled = True
+    try:
+        from . import lib
+        lib()
+    except Exception:
+        compiled = False
+    X, R, P = (np.ascontiguousarray(a, dtype=np.float64) for a in (X, R, P))
+    V = np.empty((n, 3 * m))
+    AV, BV = np.empty((n, 3 * m)), np.empty((n, 3 * m))
+    AX, BX = np.empty((n, m)), np.empty((n, m))
+    scratch = np.empty(n * 3 * m) if compiled else None
     for it in range(1, max_itr + 1):
-        V = gram_schmidt(np.hstack([X, R, P]))
-        V[:, :m] = V[:, :m] / np.linalg.norm(V[:, :m], axis=0)
-        V[:, 2 * m:] = V[:, 2 * m:] / np.linalg.norm(V[:, 2 * m:], axis=0)
-        AV = A @ V
-        BV = B @ V
+        V[:, :m] = X
+        V[:, m:2 * m] = R
+        V[:, 2 * m:] = P
+        if compiled:
+            _gram_schmidt_inplace(V, scratch)
+        else:
+            V[...] = gram_schmidt(V)
+        V[:, :m] /= np.linalg.norm(V[:, :m], axis=0)
+        V[:, 2 * m:] /= np.linalg.norm(V[:, 2 * m:], axis=0)
+        _mm_into(A, V, AV)
+        _mm_into(B, V, BV)
         b_small, lam = lapack_eig(V.T @ AV, V.T @ BV)
-        X = V @ b_small[:, :m]
-        AX = A @ X
-        BX = B @ X
-        R = AX - BX * lam[None, :m]
+        np.matmul(V, b_small[:, :m], out=X)
+        _mm_into(A, X, AX)
+        _mm_into(B, X, BX)
+        np.multiply(BX, lam[None, :m], out=R)
+        np.subtract(AX, R, out=R)
         V[:, :m] = 0.0
-        P = V @ b_small[:, :m]
-        rmax = np.abs(R).max()
+        np.matmul(V, b_small[:, :m], out=P)
+        rmax = max(float(R.max()), -float(R.min()))
         if it == 1:
             initial_R = rmax
         if progress is not None:

@@ -811,11 +811,13 @@ void orc_gram_schmidt(int64_t n, int64_t m, double *V)
 }
 
 /* The same for a row-major n x m V (numpy's C order): transposed into a
- * column-major scratch in 64-row tiles (OpenMP), orthogonalised, and
- * transposed back. */
-void orc_gram_schmidt_rm(int64_t n, int64_t m, double *V)
+ * column-major scratch T (n m doubles; NULL: allocated here) in 64-row tiles
+ * (OpenMP), orthogonalised, and transposed back.  A caller that repeats the
+ * call passes its own T: fresh pages of a large allocation cost more to
+ * fault in than the whole orthogonalisation. */
+void orc_gram_schmidt_rm(int64_t n, int64_t m, double *V, double *scratch)
 {
-    double *T = malloc((size_t)n * (size_t)m * sizeof(double));
+    double *T = scratch ? scratch : malloc((size_t)n * (size_t)m * sizeof(double));
 #pragma omp parallel for schedule(static)
     for (int64_t r0 = 0; r0 < n; r0 += 64) {
         const int64_t r1 = r0 + 64 < n ? r0 + 64 : n;
@@ -829,7 +831,7 @@ void orc_gram_schmidt_rm(int64_t n, int64_t m, double *V)
         for (int64_t r = r0; r < r1; ++r)
             for (int64_t c = 0; c < m; ++c) V[r * m + c] = T[c * n + r];
     }
-    free(T);
+    if (!scratch) free(T);
 }
 
 int orc_num_threads(void)
