@@ -1110,19 +1110,23 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-// k_residual for double-float panels: R = KX - MX diag(lam) formed in FP64
-// from the (hi, lo) pairs and stored split again; sums as k_residual.
+// k_residual for double-float panels: R = KX - MX diag(lam) in double-float
+// arithmetic on the FP32 pipe (lam split once per column); the sums of
+// |r|^2 and |m|^2 and max|r| take the leading floats (seven digits are all a
+// residual norm needs) into FP64 accumulators (no FP32 underflow of squares
+// for badly scaled systems), reduced across threads as in k_residual.
 __global__ void __launch_bounds__(kT)
     k_residual_df(int64_t n, int k, const float2 *__restrict__ KX, const float2 *__restrict__ MX,
                   const double *__restrict__ lam, float2 *__restrict__ R, double *part)
 {
     __shared__ double sred[3 * PW][kT / 32];
     const int q = blockIdx.y;
-    double rr[PW], mm[PW], mx[PW], lq[PW];
+    double rr[PW], mm[PW], mx[PW];
+    float2 lq[PW];
 #pragma unroll
     for (int c = 0; c < PW; ++c) {
         rr[c] = mm[c] = mx[c] = 0.0;
-        lq[c] = q * PW + c < k ? lam[q * PW + c] : 0.0;
+        lq[c] = q * PW + c < k ? df_split(-lam[q * PW + c]) : make_float2(0.f, 0.f);
     }
     for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
         const int64_t off = ((int64_t)q * n + row) * PW;
@@ -1135,12 +1139,16 @@ __global__ void __launch_bounds__(kT)
                 kv[c] = make_float2(0.f, 0.f);
                 continue;
             }
-            const double m = df_value(mv[c]);
-            const double r = df_value(kv[c]) - m * lq[c];
-            kv[c] = df_split(r);
-            rr[c] += r * r;
-            mm[c] += m * m;
-            mx[c] = fmax(mx[c], fabs(r));
+            DFAcc a;  // k + m (-lam)
+            a.hi = kv[c].x;
+            a.lo = kv[c].y;
+            a.add(mv[c], lq[c]);
+            const float2 r = a.get2();
+            kv[c] = r;
+            const double rd = (double)r.x, md = (double)mv[c].x;
+            rr[c] = fma(rd, rd, rr[c]);
+            mm[c] = fma(md, md, mm[c]);
+            mx[c] = fmax(mx[c], fabs(rd));
         }
         st_row(R + off, kv);
     }
