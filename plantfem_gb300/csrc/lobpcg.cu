@@ -1081,9 +1081,10 @@ __global__ void __launch_bounds__(kT)
             }
             const T r = kv[c] - mv[c] * lq[c];
             kv[c] = r;
-            rr[c] += (double)r * (double)r;
-            mm[c] += (double)mv[c] * (double)mv[c];
-            mx[c] = fmax(mx[c], fabs((double)r));
+            const double rd = (double)r, md = (double)mv[c];
+            rr[c] = fma(rd, rd, rr[c]);
+            mm[c] = fma(md, md, mm[c]);
+            mx[c] = fmax(mx[c], fabs(rd));
         }
         st_row(R + off, kv);
     }
@@ -1224,10 +1225,12 @@ __global__ void __launch_bounds__(kT)
     const int64_t n = nb * BS;
     for (int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; node < nb;
          node += (int64_t)gridDim.x * blockDim.x) {
-        double D[BS * BS];
+        // the phase's own precision: FP32 panels take the block inverse in FP32
+        using W_t = typename std::conditional<std::is_same<T, float>::value, float, double>::type;
+        W_t D[BS * BS];
 #pragma unroll
         for (int e = 0; e < BS * BS; ++e)
-            D[e] = pc == PFG_PC_NONE ? (e % (BS + 1) == 0 ? 1.0 : 0.0) : dinv[node * BS * BS + e];
+            D[e] = pc == PFG_PC_NONE ? (e % (BS + 1) == 0 ? W_t(1) : W_t(0)) : (W_t)dinv[node * BS * BS + e];
         for (int q = 0; q < np; ++q) {
             T rv[BS][PW];
 #pragma unroll
@@ -1238,9 +1241,9 @@ __global__ void __launch_bounds__(kT)
                 T wv[PW];
 #pragma unroll
                 for (int c = 0; c < PW; ++c) {
-                    double v = 0.0;
+                    W_t v = W_t(0);
 #pragma unroll
-                    for (int j = 0; j < BS; ++j) v += D[BS * i + j] * (double)rv[j][c];
+                    for (int j = 0; j < BS; ++j) v += D[BS * i + j] * (W_t)rv[j][c];
                     wv[c] = f ? T(0) : (T)v;
                 }
                 st_row(W + ((int64_t)q * n + (int64_t)BS * node + i) * PW, wv);
