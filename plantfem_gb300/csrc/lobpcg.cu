@@ -772,48 +772,37 @@ __global__ void __launch_bounds__(kT)
     }
 }
 
-template <typename T>
-struct GramAcc;
-template <>
-struct GramAcc<double> {
+struct F64Acc {
     double v;
     __device__ void zero() { v = 0.0; }
     __device__ void add(double a, double b) { v = fma(a, b, v); }
     __device__ double get() const { return v; }
 };
-template <>
-struct GramAcc<float> {
-    Comp32 v;
-    __device__ void zero() { v = Comp32{0.f, 0.f}; }
-    __device__ void add(float a, float b) { comp_add_prod(v, a, b); }
-    __device__ double get() const { return (double)v.s + (double)v.c; }
-};
-
-// Staged operand type and accumulator of the Gram kernel per storage type:
-// FP32 panels (plain or compensated FP32 sums), FP64 panels (FP64), double-
-// float panels (double-float sums).
-template <typename T, bool DF>
-struct GramArith;
-// FP32 panels (the mixed first phase, which stops at a 1e-4 residual): plain
-// FP32 multiply-adds per thread over its CTA's rows (about n / 300 terms),
-// partial sums added in FP64.  DF = true keeps the compensated FP32 form.
+// FP32 panels (the mixed first phase): plain FP32 multiply-adds per thread
+// over its CTA's rows (about n / 300 terms), partial sums added in FP64.
 struct F32Acc {
     float v;
     __device__ void zero() { v = 0.f; }
     __device__ void add(float a, float b) { v = fmaf(a, b, v); }
     __device__ double get() const { return (double)v; }
 };
-template <bool DF>
-struct GramArith<float, DF> {
+
+// Staged operand type and accumulator of the Gram kernel per storage type:
+// FP32 panels (FP32 sums), FP64 panels (FP64 sums), double-float panels
+// (double-float sums; DF = true).
+template <typename T, bool DF>
+struct GramArith;
+template <>
+struct GramArith<float, false> {
     using Stage = float;
-    using Acc = typename std::conditional<DF, GramAcc<float>, F32Acc>::type;
+    using Acc = F32Acc;
     __device__ static float stage(float x) { return x; }
     __device__ static float none() { return 0.f; }
 };
 template <>
 struct GramArith<double, false> {
     using Stage = double;
-    using Acc = GramAcc<double>;
+    using Acc = F64Acc;
     __device__ static double stage(double x) { return x; }
     __device__ static double none() { return 0.0; }
 };
