@@ -72,8 +72,10 @@ def lobpcg_crs(A, B, m: int, max_itr: int = 100000, tol: float = 1e-6, X_init=No
     """LOBPCG_CRS(A, B, lambda, X, m, MAX_ITR, TOL, X_init) with A, B scipy sparse.
 
     Convergence test as the reference: max|R| / max|R at iteration 1| < TOL
-    (SparseClass.f90:2218-2234).  ``progress(it, ratio, lam)``, if given, is
-    called after every iteration (for logging long runs).  The random start (``random%randn`` is
+    (SparseClass.f90:2218-2234).  ``progress(it, ratio, lam, R, BX)``, if
+    given, is called after every iteration (R and BX: the block's residuals and
+    B X); a true return ends the iteration there (a caller that needs only some
+    of the m pairs converged).  The random start (``random%randn`` is
     uniform, RandomClass.f90:265-283) uses a seeded numpy generator here.
     """
     n = A.shape[0]
@@ -140,8 +142,8 @@ def lobpcg_crs(A, B, m: int, max_itr: int = 100000, tol: float = 1e-6, X_init=No
         rmax = max(float(R.max()), -float(R.min()))
         if it == 1:
             initial_R = rmax
-        if progress is not None:
-            progress(it, rmax / initial_R, lam[:m])
+        if progress is not None and progress(it, rmax / initial_R, lam[:m], R, BX):
+            break  # the caller ended the iteration
         if rmax / initial_R < tol:
             break
     lam = lam[:m].copy()

@@ -210,7 +210,7 @@ def stage_cfg5(count=512, seed=5):
           dof=np.array(dofs, dtype=np.int64), E=Es, nx=nx, ny=ny, nz=nz, direct_relres=np.array(relress))
 
 
-def stage_cfg3(n=60, nev=20, block=24, tol=1e-8):
+def stage_cfg3(n=60, nev=20, block=24, tol=1e-8, pair_tol=1e-7):
     p = problems.cantilever(n)
     dom = p["domain"]
     rp, ci = O.zero_matrix(dom.nn(), dom.elemnod, 3)
@@ -223,9 +223,20 @@ def stage_cfg3(n=60, nev=20, block=24, tol=1e-8):
     B = O.CrsOperator(rm, cm, vm)
     _log(f"cfg3: reduced pencil of {A.shape[0]} DOF")
     t = time.time()
-    def progress(i, ratio, lam):
+    # The reference's rule (max|R| over all 24 block columns relative to the
+    # first iteration's < tol) waits for the 4 unwanted columns, whose
+    # eigenvalues have no gap to the rest of the spectrum; the iteration
+    # also ends once the 20 wanted pairs have relative residuals
+    # |K x - lambda M x| / |lambda M x| below pair_tol (eigenvalue errors are
+    # of the order of their squares).
+    def progress(i, ratio, lam, R, BX):
+        if i % 5:
+            return False
+        rel = np.linalg.norm(R[:, :nev], axis=0) / (np.abs(lam[:nev]) * np.linalg.norm(BX[:, :nev], axis=0))
         if i % 25 == 0:
-            _log(f"cfg3: iteration {i}, max|R| / max|R_1| {ratio:.3e}, lambda_1 {lam[0]:.10g}")
+            _log(f"cfg3: iteration {i}, max|R| / max|R_1| {ratio:.3e}, wanted pairs' max relative residual "
+                 f"{rel.max():.3e}, lambda_1 {lam[0]:.10g}")
+        return bool(rel.max() < pair_tol)
 
     lam, X, it = OL.lobpcg_crs(A, B, block, max_itr=5000, tol=tol, seed=0, return_iters=True, progress=progress)
     _log(f"cfg3: LOBPCG {it} iterations ({time.time() - t:.0f} s)")
@@ -234,7 +245,7 @@ def stage_cfg3(n=60, nev=20, block=24, tol=1e-8):
     res = np.linalg.norm(AX - BX * lam[None, :nev], axis=0) / np.linalg.norm(BX * lam[None, :nev], axis=0)
     _log(f"cfg3: lambda_1 {lam[0]:.10g}, lambda_{nev} {lam[nev - 1]:.10g}, max rel residual {res.max():.2e}")
     _save("cfg3", eigenvalues=lam[:nev], block_eigenvalues=lam, rel_residuals=res, iterations=np.int64(it),
-          ndof_reduced=np.int64(A.shape[0]), tol=np.float64(tol))
+          ndof_reduced=np.int64(A.shape[0]), tol=np.float64(tol), pair_tol=np.float64(pair_tol))
 
 
 def stage_manifest():
