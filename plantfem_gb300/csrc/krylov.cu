@@ -415,41 +415,13 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// x += alpha p_new; r -= alpha q; z = M^-1 r; rho' = r.z; rr = r.r.
-// fin (FP64): beta = rho'/rho, stop test on the recursive residual.
-// fin (FP32): same, or request a residual replacement.
-template <int BS, typename T, int QS = BS>
-__global__ void __launch_bounds__(kThreads)
-    k_cg_update(int64_t nb, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *pA, const T *pB,
-                T *__restrict__ q, const T *__restrict__ dinv, int pc, KState *S, double *pd, float *pf,
-                unsigned *ticket, double tol, double delta, int itrmax)
+// The end of a CG update pass: the grid totals rho' = <r, z> and <r, r>, then
+// (last CTA only) fin (FP64): beta = rho'/rho, stop test on the recursive
+// residual; fin (FP32): the same, or request a residual replacement.
+template <typename T>
+__device__ __forceinline__ void cg_update_tail(typename Acc<T>::type (&acc)[2], KState *S, double *pd, float *pf,
+                                               unsigned *ticket, double tol, double delta, int itrmax)
 {
-    if (S->done | S->need_update) return;
-    const T alpha = st_alpha<T>(S);
-    const T *pnew = S->parity ? pA : pB;
-    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
-    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
-         row += (int64_t)gridDim.x * blockDim.x) {
-        T rv[BS], zv[BS];
-#pragma unroll
-        for (int i = 0; i < BS; ++i) {
-            const int64_t j = (int64_t)BS * row + i;
-            x[j] = fma(alpha, pnew[j], x[j]);
-            rv[i] = fma(-alpha, q[(int64_t)QS * row + i], r[j]);
-            r[j] = rv[i];
-        }
-        if (QS == 4) {  // the symmetric product's accumulator: cleared for the next product
-#pragma unroll
-            for (int i = 0; i < 4; ++i) q[4 * row + i] = T(0);
-        }
-        pc_apply<BS, T>(pc, dinv, row, rv, zv);
-#pragma unroll
-        for (int i = 0; i < BS; ++i) {
-            z[(int64_t)BS * row + i] = zv[i];
-            Acc<T>::add(acc[0], rv[i], zv[i]);
-            Acc<T>::add(acc[1], rv[i], rv[i]);
-        }
-    }
     T tot[2];
     if (grid_total<2>(acc, pd, pf, ticket, tot)) {
         S->iter += 1;
@@ -493,6 +465,42 @@ __global__ void __launch_bounds__(kThreads)
             S->done = 1;
         }
     }
+}
+
+// x += alpha p_new; r -= alpha q; z = M^-1 r; rho' = r.z; rr = r.r.
+template <int BS, typename T, int QS = BS>
+__global__ void __launch_bounds__(kThreads)
+    k_cg_update(int64_t nb, T *__restrict__ x, T *__restrict__ r, T *__restrict__ z, const T *pA, const T *pB,
+                T *__restrict__ q, const T *__restrict__ dinv, int pc, KState *S, double *pd, float *pf,
+                unsigned *ticket, double tol, double delta, int itrmax)
+{
+    if (S->done | S->need_update) return;
+    const T alpha = st_alpha<T>(S);
+    const T *pnew = S->parity ? pA : pB;
+    typename Acc<T>::type acc[2] = {Acc<T>::zero(), Acc<T>::zero()};
+    for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < nb;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        T rv[BS], zv[BS];
+#pragma unroll
+        for (int i = 0; i < BS; ++i) {
+            const int64_t j = (int64_t)BS * row + i;
+            x[j] = fma(alpha, pnew[j], x[j]);
+            rv[i] = fma(-alpha, q[(int64_t)QS * row + i], r[j]);
+            r[j] = rv[i];
+        }
+        if (QS == 4) {  // the symmetric product's accumulator: cleared for the next product
+#pragma unroll
+            for (int i = 0; i < 4; ++i) q[4 * row + i] = T(0);
+        }
+        pc_apply<BS, T>(pc, dinv, row, rv, zv);
+#pragma unroll
+        for (int i = 0; i < BS; ++i) {
+            z[(int64_t)BS * row + i] = zv[i];
+            Acc<T>::add(acc[0], rv[i], zv[i]);
+            Acc<T>::add(acc[1], rv[i], rv[i]);
+        }
+    }
+    cg_update_tail<T>(acc, S, pd, pf, ticket, tol, delta, itrmax);
 }
 
 // (Re)start of CG from the residual r: z = M^-1 r, rho = r.z, beta = 0.
