@@ -210,7 +210,20 @@ def stage_cfg5(count=512, seed=5):
           dof=np.array(dofs, dtype=np.int64), E=Es, nx=nx, ny=ny, nz=nz, direct_relres=np.array(relress))
 
 
-def stage_cfg3(n=60, nev=20, block=24, tol=1e-8, pair_tol=1e-7):
+def stage_cfg3(n=60, nev=20, block=24, pair_tol=1e-8, chunk=100, max_chunks=40):
+    """The lowest 20 pairs of the 60^3 cantilever pencil (K, M) with the
+    fix_eig DOFs removed, by SciPy's LOBPCG (Knyazev's method with a
+    B-orthonormal basis) on the oracle's assembled and reduced matrices, point
+    Jacobi preconditioned, run in chunks until the 20 wanted pairs have
+    relative residuals |K x - lambda M x| / |lambda M x| <= pair_tol.
+
+    The restatement of the reference's LOBPCG_CRS (oracle/lobpcg.py:
+    Euclidean Gram-Schmidt of [X R P], no preconditioner) stagnates on this
+    pencil: 450 iterations left the worst wanted pair at a 7e-3 relative
+    residual (3.4 s per iteration on 8 cores), far from the 1e-8 the
+    configuration asks; the eigenvalues are properties of the pencil, so an
+    independent converged solver pins them."""
+    import scipy.sparse.linalg as sla_
     p = problems.cantilever(n)
     dom = p["domain"]
     rp, ci = O.zero_matrix(dom.nn(), dom.elemnod, 3)
@@ -221,31 +234,37 @@ def stage_cfg3(n=60, nev=20, block=24, tol=1e-8, pair_tol=1e-7):
     del K, M, rp, ci
     A = O.CrsOperator(rk, ck, vk)
     B = O.CrsOperator(rm, cm, vm)
-    _log(f"cfg3: reduced pencil of {A.shape[0]} DOF")
-    t = time.time()
-    # The reference's rule (max|R| over all 24 block columns relative to the
-    # first iteration's < tol) waits for the 4 unwanted columns, whose
-    # eigenvalues have no gap to the rest of the spectrum; the iteration
-    # also ends once the 20 wanted pairs have relative residuals
-    # |K x - lambda M x| / |lambda M x| below pair_tol (eigenvalue errors are
-    # of the order of their squares).
-    def progress(i, ratio, lam, R, BX):
-        if i % 5:
-            return False
-        rel = np.linalg.norm(R[:, :nev], axis=0) / (np.abs(lam[:nev]) * np.linalg.norm(BX[:, :nev], axis=0))
-        if i % 25 == 0:
-            _log(f"cfg3: iteration {i}, max|R| / max|R_1| {ratio:.3e}, wanted pairs' max relative residual "
-                 f"{rel.max():.3e}, lambda_1 {lam[0]:.10g}")
-        return bool(rel.max() < pair_tol)
+    nred = A.shape[0]
+    dinv = 1.0 / O.crs_to_scipy(rk, ck, vk).diagonal()
+    _log(f"cfg3: reduced pencil of {nred} DOF")
 
-    lam, X, it = OL.lobpcg_crs(A, B, block, max_itr=5000, tol=tol, seed=0, return_iters=True, progress=progress)
-    _log(f"cfg3: LOBPCG {it} iterations ({time.time() - t:.0f} s)")
-    # relative residuals of the wanted pairs, |K x - lambda M x| / |lambda M x|
-    AX, BX = A @ X[:, :nev], B @ X[:, :nev]
-    res = np.linalg.norm(AX - BX * lam[None, :nev], axis=0) / np.linalg.norm(BX * lam[None, :nev], axis=0)
-    _log(f"cfg3: lambda_1 {lam[0]:.10g}, lambda_{nev} {lam[nev - 1]:.10g}, max rel residual {res.max():.2e}")
-    _save("cfg3", eigenvalues=lam[:nev], block_eigenvalues=lam, rel_residuals=res, iterations=np.int64(it),
-          ndof_reduced=np.int64(A.shape[0]), tol=np.float64(tol), pair_tol=np.float64(pair_tol))
+    def lin(op):
+        return sla_.LinearOperator((nred, nred), matvec=lambda v: op @ np.asarray(v).reshape(-1),
+                                   matmat=lambda X: op @ np.ascontiguousarray(X), dtype=np.float64)
+
+    Aop, Bop = lin(A), lin(B)
+    Pop = sla_.LinearOperator((nred, nred), matvec=lambda v: dinv * np.asarray(v).reshape(-1),
+                              matmat=lambda X: dinv[:, None] * X, dtype=np.float64)
+    X = np.random.default_rng(0).random((nred, block))
+    t = time.time()
+    its = 0
+    import warnings
+    for c in range(max_chunks):
+        with warnings.catch_warnings():  # each chunk ends "not reaching the requested tolerance" by design
+            warnings.simplefilter("ignore", UserWarning)
+            lam, X = sla_.lobpcg(Aop, X, B=Bop, M=Pop, tol=1e-30, maxiter=chunk, largest=False)
+        its += chunk
+        order = np.argsort(lam)
+        lam, X = lam[order], X[:, order]
+        AX, BX = A @ np.ascontiguousarray(X[:, :nev]), B @ np.ascontiguousarray(X[:, :nev])
+        res = np.linalg.norm(AX - BX * lam[None, :nev], axis=0) / np.linalg.norm(BX * lam[None, :nev], axis=0)
+        _log(f"cfg3: {its} iterations, wanted pairs' max relative residual {res.max():.3e}, "
+             f"lambda_1 {lam[0]:.12g}, lambda_{nev} {lam[nev - 1]:.12g} ({time.time() - t:.0f} s)")
+        if res.max() <= pair_tol:
+            break
+    assert res.max() <= pair_tol, res.max()
+    _save("cfg3", eigenvalues=lam[:nev], block_eigenvalues=lam, rel_residuals=res, iterations=np.int64(its),
+          ndof_reduced=np.int64(nred), pair_tol=np.float64(pair_tol))
 
 
 def stage_manifest():

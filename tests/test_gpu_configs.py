@@ -13,7 +13,10 @@ SHA-256 in its MANIFEST.json), so these tests run only the CUDA path:
   BiCGSTAB (symmetric FP32 copy) within 1e-8 on a 50,000-entry seeded sample
   and in norm, fixed DOFs exactly zero;
 * config 3 (60^3 cantilever): the lowest 20 eigenvalues, FP64 and mixed
-  LOBPCG (block 24, tol 1e-8), within 1e-7 relative of the oracle's LOBPCG_CRS;
+  LOBPCG (block 24, tol 1e-8), within 1e-7 relative of the eigenvalues of the
+  oracle's assembled and reduced pencil, converged to 1e-8 relative residuals
+  by SciPy's LOBPCG (the reference's LOBPCG_CRS restated stagnates near 7e-3
+  on this pencil);
 * config 4 (64^3, 262,144 per-element E): the adjoint gradient dL/dE, FP64 and
   mixed, within 1e-7 of the largest gradient entry at the 32 finite-difference
   elements and 4,096 more;
@@ -140,7 +143,7 @@ def test_config2_full_size_vs_oracle(cuda, config2, algorithm, precision, storag
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_config3_eigenvalues_vs_oracle(cuda, precision):
     if "cfg3.npz" not in json.load(open(os.path.join(CFG, "MANIFEST.json")))["files"]:
-        pytest.skip("the oracle's 60^3 LOBPCG fixture (tests/golden/make_config_fixtures.py cfg3) is not generated")
+        pytest.skip("the 60^3 eigenvalue fixture (tests/golden/make_config_fixtures.py cfg3) is not generated")
     ref = _fixture("cfg3")
     p = problems.cantilever(60)
     s = FEMSolver()
