@@ -296,17 +296,31 @@ static void sym_eig_lowest(int n, std::vector<double> &A, int k, std::vector<dou
             for (int i = 0; i < n; ++i) x[i] /= nrm;
         }
         std::copy(x.begin(), x.end(), Yt.begin() + (size_t)j * n);
-        // back transformation: y <- H_0 (H_1 (... (H_{n-3} y)))
-        for (int jj = n - 3; jj >= 0; --jj) {
-            if (beta[jj] == 0.0) continue;
-            const double *vj = &V[(size_t)jj * n];
-            double s = 0.0;
-            for (int i = jj + 1; i < n; ++i) s += vj[i] * x[i];
-            s *= beta[jj];
-            for (int i = jj + 1; i < n; ++i) x[i] -= s * vj[i];
-        }
-        std::copy(x.begin(), x.end(), Y.begin() + (size_t)j * n);
     }
+    // back transformation of all kk vectors at once, y <- H_0 (H_1 (... (H_{n-3} y))):
+    // the block is held row-major (n x kk), so each reflector's dot products
+    // and updates run along contiguous rows of kk values
+    std::vector<double> Xr((size_t)n * kk), sv(kk);
+    for (int c = 0; c < kk; ++c)
+        for (int i = 0; i < n; ++i) Xr[(size_t)i * kk + c] = Yt[(size_t)c * n + i];
+    for (int jj = n - 3; jj >= 0; --jj) {
+        if (beta[jj] == 0.0) continue;
+        const double *vj = &V[(size_t)jj * n];
+        for (int c = 0; c < kk; ++c) sv[c] = 0.0;
+        for (int i = jj + 1; i < n; ++i) {
+            const double vi = vj[i];
+            const double *xi = &Xr[(size_t)i * kk];
+            for (int c = 0; c < kk; ++c) sv[c] += vi * xi[c];
+        }
+        for (int c = 0; c < kk; ++c) sv[c] *= beta[jj];
+        for (int i = jj + 1; i < n; ++i) {
+            const double vi = vj[i];
+            double *xi = &Xr[(size_t)i * kk];
+            for (int c = 0; c < kk; ++c) xi[c] -= sv[c] * vi;
+        }
+    }
+    for (int c = 0; c < kk; ++c)
+        for (int i = 0; i < n; ++i) Y[(size_t)c * n + i] = Xr[(size_t)i * kk + c];
 }
 
 // B = L L^T (lower L, column-major, in place of B's lower triangle) when every
@@ -354,53 +368,57 @@ int small_generalized_eig(int m, const double *Ain, const double *Bin, int k, do
         // Otherwise B's eigendecomposition below drops its null directions.
         std::vector<double> L = B;
         if (cholesky_well_posed(m, L, rank_tol)) {
-            // column-oriented forward substitution: x <- L^-1 x (each step a
-            // contiguous axpy down column q of L)
-            auto lsolve = [&](double *x) {
+            // Block forward substitution X <- L^-1 X on a row-major m x w
+            // block: each step scales row q and subtracts it from the rows
+            // below, whole rows at a time (contiguous, vectorisable).
+            auto block_lsolve = [&](double *X, int w) {
                 for (int q = 0; q < m; ++q) {
-                    const double *lq = &L[(size_t)q * m];
-                    const double xq = x[q] / lq[q];
-                    x[q] = xq;
-                    for (int i = q + 1; i < m; ++i) x[i] -= lq[i] * xq;
+                    const double *lq = &L[(size_t)q * m];  // column q of L
+                    double *xq = X + (size_t)q * w;
+                    const double inv = 1.0 / lq[q];
+                    for (int c = 0; c < w; ++c) xq[c] *= inv;
+                    for (int i = q + 1; i < m; ++i) {
+                        const double f = lq[i];
+                        double *xi = X + (size_t)i * w;
+                        for (int c = 0; c < w; ++c) xi[c] -= f * xq[c];
+                    }
                 }
             };
-            // W = L^-1 (S A S), column by column
+            // W = L^-1 (S A S); A' = W L^-T = (L^-1 W^T)^T (symmetric)
             std::vector<double> W((size_t)m * m), Ap((size_t)m * m);
-            for (int c = 0; c < m; ++c) {
-                double *wc = &W[(size_t)c * m];
-                for (int i = 0; i < m; ++i) wc[i] = 0.5 * (Ain[(size_t)c * m + i] + Ain[(size_t)i * m + c]) * s[i] * s[c];
-                lsolve(wc);
-            }
-            // A' = W L^-T = (L^-1 W^T)^T: the columns of W^T, solved, are A''s rows
-            for (int r = 0; r < m; ++r) {
-                double *ar = &Ap[(size_t)r * m];
-                for (int i = 0; i < m; ++i) ar[i] = W[(size_t)i * m + r];
-                lsolve(ar);
-            }
-            for (int c = 0; c < m; ++c)  // (Ap holds A'^T; symmetrise)
-                for (int i = 0; i < c; ++i) {
-                    const double v = 0.5 * (Ap[(size_t)c * m + i] + Ap[(size_t)i * m + c]);
-                    Ap[(size_t)c * m + i] = Ap[(size_t)i * m + c] = v;
+            for (int r = 0; r < m; ++r)
+                for (int c = 0; c < m; ++c)
+                    W[(size_t)r * m + c] = 0.5 * (Ain[(size_t)c * m + r] + Ain[(size_t)r * m + c]) * s[r] * s[c];
+            block_lsolve(W.data(), m);
+            for (int r = 0; r < m; ++r)
+                for (int c = 0; c < m; ++c) Ap[(size_t)r * m + c] = W[(size_t)c * m + r];
+            block_lsolve(Ap.data(), m);
+            for (int c = 0; c < m; ++c)  // symmetrise
+                for (int r = 0; r < c; ++r) {
+                    const double v = 0.5 * (Ap[(size_t)c * m + r] + Ap[(size_t)r * m + c]);
+                    Ap[(size_t)c * m + r] = Ap[(size_t)r * m + c] = v;
                 }
-            std::vector<double> LT((size_t)m * m);  // L^T, for column-oriented back substitution
-            for (int c = 0; c < m; ++c)
-                for (int i = 0; i < m; ++i) LT[(size_t)i * m + c] = L[(size_t)c * m + i];
             std::vector<double> mu, Y;
             const int kk = std::min(k, m);
             sym_eig_lowest(m, Ap, kk, mu, Y);
-            for (int j = 0; j < kk; ++j) {
-                lam[j] = mu[j];
-                // y = column j of the eigenvectors; C_j = S L^-T y (back
-                // substitution on L^T, column-oriented)
-                double *cj = C + (size_t)j * m;
-                for (int i = 0; i < m; ++i) cj[i] = Y[(size_t)j * m + i];
-                for (int i = m - 1; i >= 0; --i) {
-                    const double *lti = &LT[(size_t)i * m];
-                    const double ci = cj[i] / lti[i];
-                    cj[i] = ci;
-                    for (int q = 0; q < i; ++q) cj[q] -= lti[q] * ci;
+            // C = S L^-T Y: block back substitution on the row-major m x kk
+            // block of the eigenvectors
+            std::vector<double> Cb((size_t)m * kk);
+            for (int j2 = 0; j2 < kk; ++j2)
+                for (int r = 0; r < m; ++r) Cb[(size_t)r * kk + j2] = Y[(size_t)j2 * m + r];
+            for (int r = m - 1; r >= 0; --r) {
+                double *cr = &Cb[(size_t)r * kk];
+                const double inv = 1.0 / L[(size_t)r * m + r];
+                for (int c = 0; c < kk; ++c) cr[c] *= inv;
+                for (int q = 0; q < r; ++q) {
+                    const double f = L[(size_t)q * m + r];  // L(r, q) = L^T(q, r)
+                    double *cq = &Cb[(size_t)q * kk];
+                    for (int c = 0; c < kk; ++c) cq[c] -= f * cr[c];
                 }
-                for (int i = 0; i < m; ++i) cj[i] *= s[i];
+            }
+            for (int j2 = 0; j2 < kk; ++j2) {
+                lam[j2] = mu[j2];
+                for (int r = 0; r < m; ++r) C[(size_t)j2 * m + r] = Cb[(size_t)r * kk + j2] * s[r];
             }
             return kk;
         }
