@@ -264,6 +264,7 @@ static void sym_eig_lowest(int n, std::vector<double> &A, int k, std::vector<dou
             }
         }
         if (std::fabs(dg[n - 1]) < tiny) dg[n - 1] = dg[n - 1] < 0 ? -tiny : tiny;
+        for (int i = 0; i < n; ++i) dg[i] = 1.0 / dg[i];  // pivots kept as reciprocals for the solves
         // start: a fixed pseudo-random vector (different per j)
         for (int i = 0; i < n; ++i) {
             uint64_t h = (uint64_t)(j + 1) * 0x9e3779b97f4a7c15ull ^ ((uint64_t)i * 0xbf58476d1ce4e5b9ull);
@@ -281,7 +282,7 @@ static void sym_eig_lowest(int n, std::vector<double> &A, int k, std::vector<dou
                 double t = x[i];
                 if (i + 1 < n) t -= du[i] * x[i + 1];
                 if (i + 2 < n) t -= du2[i] * x[i + 2];
-                x[i] = t / dg[i];
+                x[i] = t * dg[i];
             }
             for (int c = cluster0; c < j; ++c) {  // orthogonal to the cluster's earlier vectors
                 const double *yc = &Yt[(size_t)c * n];
