@@ -76,6 +76,21 @@ def test_symmetric_cg_fused_direction_matches_oracle(cuda, pc):
     assert _rel(x, xo) <= 1e-8, _rel(x, xo)
 
 
+@pytest.mark.parametrize("n", [1, 2, 3])
+@pytest.mark.parametrize("algorithm", ["CG", "BiCGSTAB"])
+def test_symmetric_storage_tiny_meshes(cuda, n, algorithm):
+    """One partial slice (8, 27 or 64 nodes: fewer block rows than the 32 of a
+    slice, most warps of the staged products without a slice): the
+    shared-memory staging still matches the oracle."""
+    p, xo = _system(n, seed=100 + n)
+    s = _solver(p)
+    s.relative_er = 1e-12
+    x = s.solve(algorithm=algorithm, preconditioning="BlockJacobi", precision="mixed", stop_rule="true_relative",
+                storage="symmetric")
+    assert s.last_info["status"] == 0, s.last_info
+    assert _rel(x, xo) <= 1e-8, _rel(x, xo)
+
+
 def test_symmetric_storage_larger_mesh_twice(cuda):
     """30^3: two symmetric-storage mixed CG solves in a row reach 1e-10 and
     agree with the FP64 GPU solve to 1e-8 (the second reuses the upper copy)."""
