@@ -621,11 +621,10 @@ def adjoint_lines(n=64, n_fd=32, tol=1e-10):
 def e2e_line(args, ws, s, stage, x64_host):
     """End to end through the C ABI plug-in (pfg_linear_solver_crs) with host
     (pinned) CRS arrays: every call copies the CRS in and the solution out.
-    Run right after the timed solves: later in a long process (after the
-    BiCGSTAB and variant sections) the pinned host-to-device copies were
-    measured at 19-58 GB/s instead of 197-211 GB/s in some runs (cause not
-    identified), which would charge the plug-in for the state the rest of the
-    benchmark leaves behind."""
+    Run right after the timed solves.  The pinned host-to-device copies run at
+    the link's ~211 GB/s or, in phases that come and go between calls and
+    between runs, at ~20-60 GB/s (cause not identified); `ms_each` and
+    `pinned_h2d_GBs` record which."""
     import torch
     from plantfem_gb300 import linear_solver_crs
     e2e = None
